@@ -1,0 +1,107 @@
+// si_device.h — structures shared by the host runtime (si_runtime.cpp) and the kernels (*.cu).
+//
+// HBM layout of one scene:
+//   particles: two buffers (ping-pong for the sort), each 8 SoA streams of float4 with stride `cap`
+//              (stream k = vec4 k of the reference record: x, v, c0, c1, c2, f0, f1, f2);
+//   grid:      two node arrays of int4 (ping-pong: P2G of substep s+1 is fused into the G2P of
+//              substep s and lands in the other array, which the grid update of s cleared);
+//   keys:      u32 per particle (block key of the last sort, pre-sort order, mpm.js:569);
+//   starts:    u32 x (num_blocks + 1) (mpm.js:122, after the scan).
+// A tick is one substep of every scene that has work. The host builds one TickScene per such
+// scene; kernels map a flat chunk index to its scene by binary search over the chunk prefixes.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace si {
+
+constexpr int kStreams = 8;           // float4 streams per particle
+constexpr int kCtaThreads = 256;      // threads per CTA of the particle kernels
+constexpr int kMaxPpt = 4;            // particles per thread in one chunk, at most
+constexpr int kNodeChunk = 2048;      // grid nodes per work item of the grid kernel
+constexpr int kSortTile = 4096;       // keys per CTA of a radix pass (256 threads x 16)
+constexpr int kRadixBits = 8;
+
+// TickScene.flags
+constexpr uint32_t F_P2G = 1u;        // run a standalone P2G into `grid` this substep
+constexpr uint32_t F_GATHER = 2u;     // this substep sorts: G2P (or the reorder) reads P[perm] and writes Palt
+constexpr uint32_t F_FUSE = 4u;       // G2P also scatters the new particle state into grid_next
+constexpr uint32_t F_KEYS = 8u;       // G2P also writes the block key of the new position
+constexpr uint32_t F_FORCE_GLOBAL = 16u; // P2G skips the shared-memory tile (mpm.js:380)
+constexpr uint32_t F_NO_CLEAR_NEXT = 32u; // grid update leaves grid_next alone
+constexpr uint32_t F_KEYS_NOW = 64u;  // compute the block keys of the current positions before the sort
+constexpr uint32_t F_CLEAR = 128u;    // zero `grid` before the standalone P2G
+
+struct SceneParams {             // per scene, device resident, rewritten when a value changes
+  float4 mats[24];               // 8 materials x 3 vec4 (mpm.js:116)
+  float4 cols[48];               // 16 colliders x 3 vec4 (mpm.js:117)
+  int32_t dims[3];
+  int32_t ncol;
+  float gravity[3];              // lattice units per substep^2 at the scene's dt
+  float bound;                   // 3
+  float floor_friction;          // 0.4
+  float vmax;                    // 0.9
+  float vol4;                    // 4 / ppcAxis^3
+  uint32_t num_blocks;
+};
+
+struct TickScene {               // per tick and active scene, host built
+  const SceneParams* prm;
+  float4* P;                     // particle state read this substep (current buffer)
+  float4* Palt;                  // destination of the sort's gather
+  int4* grid;                    // grid of this substep
+  int4* grid_next;               // grid of the next substep
+  uint32_t* keys;                // per-scene key array (pre-sort order)
+  uint32_t* starts;              // per-scene starts (num_blocks + 1)
+  int64_t cap;                   // stream stride in float4
+  int32_t n;                     // particles
+  uint32_t flags;
+  uint32_t seg_base;             // first slot of this scene in the concatenated sort arrays
+  uint32_t bin_base;             // first global bin of this scene
+  uint32_t pchunk_begin;         // first particle chunk of this scene (prefix over the tick)
+  uint32_t nchunk_begin;         // first node chunk
+};
+
+struct TickInfo {                // one tick's totals (kernel arguments)
+  const TickScene* ts;
+  int32_t nscenes;
+  uint32_t pchunks;              // particle chunks of all scenes
+  uint32_t nchunks;              // node chunks
+  int32_t chunk;                 // particles per chunk (= kCtaThreads * ppt)
+  int32_t tile_nodes;            // shared tile capacity in nodes
+};
+
+struct SortInfo {                // one tick's sort
+  uint32_t n;                    // elements = particles of the sorting scenes
+  uint32_t bins;                 // total bins
+  int32_t passes;
+  uint32_t* keys_a; uint32_t* vals_a;
+  uint32_t* keys_b; uint32_t* vals_b;
+  uint32_t* hist;                // 256 x tiles
+  uint32_t* digit_total;         // 256
+};
+
+// ---- launchers (si_kernels.cu / si_sort.cu); all enqueue on `st`.
+void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st);
+void launch_clear(const TickInfo& t, int grid_ctas, cudaStream_t st);
+void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st);
+void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
+void launch_reorder(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
+void launch_keys(const TickInfo& t, int grid_ctas, cudaStream_t st);
+void launch_retime(float4* P, int64_t cap, int32_t n, float k, cudaStream_t st);
+void launch_aos_to_soa(const float* aos, float4* P, int64_t cap, int64_t off, int64_t n, cudaStream_t st);
+void launch_soa_to_aos(const float4* P, int64_t cap, int64_t off, int64_t n, float* aos, cudaStream_t st);
+void launch_positions(const float4* P, int64_t cap, int64_t off, int64_t n, double dx,
+                      const double origin[3], float* xyz, cudaStream_t st);
+// Sort of one tick: builds the concatenated (key, index) arrays of the sorting scenes, radix
+// sorts them and leaves perm (sorted source indices, per segment) in *perm_out and the sorted
+// keys in *keys_out.
+void launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out,
+                 const uint32_t** keys_out, int grid_ctas, cudaStream_t st);
+// Per-scene starts (reference blockCount after the scan) of every sorting scene.
+void launch_scene_starts_all(const TickInfo& t, const uint32_t* sorted_keys, uint32_t max_blocks,
+                             cudaStream_t st);
+int p2g_smem_bytes(int tile_nodes);
+int occupancy_ctas(int which, int tile_nodes);   // resident CTAs per SM of kernel `which`
+
+}  // namespace si

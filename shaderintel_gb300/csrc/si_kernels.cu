@@ -1,0 +1,649 @@
+// si_kernels.cu — the substep kernels for sm_103a: P2G (tile / global, optional sort gather),
+// grid update, G2P (with the next substep's P2G and block keys fused in), retime, record I/O.
+//
+// Built with -fmad=false: the f32 order of si_math.cuh is the contract with the CPU oracle.
+// Work mapping: persistent CTAs walk flat chunk indices of one tick; a chunk belongs to one scene
+// (binary search over the prefixes the host wrote), so one launch per phase serves every scene.
+#include <algorithm>
+
+#include "si_device.h"
+#include "si_math.cuh"
+#include "si_runtime.h"
+
+namespace si {
+
+__device__ __forceinline__ int find_scene_p(const TickScene* ts, int n, uint32_t chunk) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (ts[mid].pchunk_begin <= chunk) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ int find_scene_n(const TickScene* ts, int n, uint32_t chunk) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (ts[mid].nchunk_begin <= chunk) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ------------------------------------------------------------------ P2G inputs of one particle
+struct Scat {
+  int32_t b[3];      // base node
+  float f[3];        // fx = x - base
+  float aff[9];      // affine = -vol4 tau + m C, column-major
+  float mv[3];       // m v
+  float mass;
+};
+
+__device__ __forceinline__ void prep_scatter(Scat& s, float4 x, float4 v, float4 c0, float4 c1, float4 c2,
+                                             float t01, float t02, float t12, const SceneParams* prm) {
+  s.b[0] = base_of(x.x, prm->dims[0]);
+  s.b[1] = base_of(x.y, prm->dims[1]);
+  s.b[2] = base_of(x.z, prm->dims[2]);
+  s.f[0] = x.x - (float)s.b[0];
+  s.f[1] = x.y - (float)s.b[1];
+  s.f[2] = x.z - (float)s.b[2];
+  uint32_t mid = __float_as_uint(x.w) & 7u;
+  float mass = __ldg(&prm->mats[mid * 3].y);
+  s.mass = mass;
+  float nv = -prm->vol4;
+  // tau columns (tau00 tau01 tau02), (tau01 tau11 tau12), (tau02 tau12 tau22): mpm.js:324
+  s.aff[0] = nv * c0.w + mass * c0.x;
+  s.aff[1] = nv * t01 + mass * c0.y;
+  s.aff[2] = nv * t02 + mass * c0.z;
+  s.aff[3] = nv * t01 + mass * c1.x;
+  s.aff[4] = nv * c1.w + mass * c1.y;
+  s.aff[5] = nv * t12 + mass * c1.z;
+  s.aff[6] = nv * t02 + mass * c2.x;
+  s.aff[7] = nv * t12 + mass * c2.y;
+  s.aff[8] = nv * c2.w + mass * c2.z;
+  s.mv[0] = mass * v.x;
+  s.mv[1] = mass * v.y;
+  s.mv[2] = mass * v.z;
+}
+
+__device__ __forceinline__ bool in_grid(int gx, int gy, int gz, const int32_t* d) {
+  return (unsigned)gx < (unsigned)d[0] && (unsigned)gy < (unsigned)d[1] && (unsigned)gz < (unsigned)d[2];
+}
+
+// 27-node scatter of mpm.js:328-349 into the shared tile (planar channels) or the global grid.
+__device__ __forceinline__ void scatter_one(const Scat& s, const int32_t* dims, int* __restrict__ grid,
+                                            int* tile, int tile_cap, int o0, int o1, int o2, int ex, int ey,
+                                            bool use_tile) {
+  float wx[3], wy[3], wz[3];
+  bspline(s.f[0], wx); bspline(s.f[1], wy); bspline(s.f[2], wz);
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    float dx = (float)a - s.f[0];
+    float ax0 = s.aff[0] * dx, ax1 = s.aff[1] * dx, ax2 = s.aff[2] * dx;
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+      float dy = (float)b - s.f[1];
+      float wab = wx[a] * wy[b];
+      float s0 = ax0 + s.aff[3] * dy, s1 = ax1 + s.aff[4] * dy, s2 = ax2 + s.aff[5] * dy;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        float dz = (float)c - s.f[2];
+        float wt = wab * wz[c];
+        float r0 = s0 + s.aff[6] * dz, r1 = s1 + s.aff[7] * dz, r2 = s2 + s.aff[8] * dz;
+        int32_t q0 = to_fixed(wt * (s.mv[0] + r0));
+        int32_t q1 = to_fixed(wt * (s.mv[1] + r1));
+        int32_t q2 = to_fixed(wt * (s.mv[2] + r2));
+        int32_t q3 = to_fixed(wt * s.mass);
+        int gx = s.b[0] + a, gy = s.b[1] + b, gz = s.b[2] + c;
+        if (use_tile) {
+          int ti = ((gz - o2) * ey + (gy - o1)) * ex + (gx - o0);
+          atomicAdd(&tile[ti], q0);
+          atomicAdd(&tile[tile_cap + ti], q1);
+          atomicAdd(&tile[2 * tile_cap + ti], q2);
+          atomicAdd(&tile[3 * tile_cap + ti], q3);
+        } else if (in_grid(gx, gy, gz, dims)) {
+          size_t gi = 4 * ((size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz));
+          atomicAdd(&grid[gi], q0);
+          atomicAdd(&grid[gi + 1], q1);
+          atomicAdd(&grid[gi + 2], q2);
+          atomicAdd(&grid[gi + 3], q3);
+        }
+      }
+    }
+  }
+}
+
+// CTA-wide P2G of up to PPT particles per thread: AABB of the bases (mpm.js:353-377), tile if it
+// fits (mpm.js:379-380), scatter, flush of the non-zero tile nodes with global i32 atomics (mpm.js:385-399).
+template <int PPT>
+__device__ __forceinline__ void cta_scatter(const Scat (&s)[PPT], const bool (&valid)[PPT], const int32_t* dims,
+                                            int* __restrict__ grid, bool force_global, int tile_cap,
+                                            int* tile, int* sbox) {
+  const int tid = threadIdx.x;
+  if (tid < 3) { sbox[tid] = 0x3fffffff; sbox[3 + tid] = -0x3fffffff; }
+  __syncthreads();
+  int lo0 = 0x3fffffff, lo1 = 0x3fffffff, lo2 = 0x3fffffff;
+  int hi0 = -0x3fffffff, hi1 = -0x3fffffff, hi2 = -0x3fffffff;
+#pragma unroll
+  for (int k = 0; k < PPT; k++) {
+    if (valid[k]) {
+      lo0 = min(lo0, s[k].b[0]); lo1 = min(lo1, s[k].b[1]); lo2 = min(lo2, s[k].b[2]);
+      hi0 = max(hi0, s[k].b[0]); hi1 = max(hi1, s[k].b[1]); hi2 = max(hi2, s[k].b[2]);
+    }
+  }
+  lo0 = __reduce_min_sync(0xffffffffu, lo0); lo1 = __reduce_min_sync(0xffffffffu, lo1);
+  lo2 = __reduce_min_sync(0xffffffffu, lo2);
+  hi0 = __reduce_max_sync(0xffffffffu, hi0); hi1 = __reduce_max_sync(0xffffffffu, hi1);
+  hi2 = __reduce_max_sync(0xffffffffu, hi2);
+  if ((tid & 31) == 0) {
+    atomicMin(&sbox[0], lo0); atomicMin(&sbox[1], lo1); atomicMin(&sbox[2], lo2);
+    atomicMax(&sbox[3], hi0); atomicMax(&sbox[4], hi1); atomicMax(&sbox[5], hi2);
+  }
+  __syncthreads();
+  const int o0 = sbox[0], o1 = sbox[1], o2 = sbox[2];
+  const int ex = sbox[3] - o0 + 3, ey = sbox[4] - o1 + 3, ez = sbox[5] - o2 + 3;
+  __syncthreads();   // sbox is reused by the next chunk
+  if (ex <= 0 || ey <= 0 || ez <= 0) return;    // no valid particle in the chunk
+  const long long tn = (long long)ex * ey * ez;
+  const bool use_tile = tn <= tile_cap && !force_global;
+  const int tnodes = (int)(use_tile ? tn : 0);
+  if (use_tile) {
+    for (int t = tid; t < tnodes; t += blockDim.x) {
+      tile[t] = 0; tile[tile_cap + t] = 0; tile[2 * tile_cap + t] = 0; tile[3 * tile_cap + t] = 0;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < PPT; k++)
+    if (valid[k]) scatter_one(s[k], dims, grid, tile, tile_cap, o0, o1, o2, ex, ey, use_tile);
+  if (use_tile) {
+    __syncthreads();
+    for (int t = tid; t < tnodes; t += blockDim.x) {
+      int m = tile[3 * tile_cap + t], mx = tile[t], my = tile[tile_cap + t], mz = tile[2 * tile_cap + t];
+      if ((m | mx | my | mz) != 0) {
+        int lx = t % ex, ly = (t / ex) % ey, lz = t / (ex * ey);
+        int gx = o0 + lx, gy = o1 + ly, gz = o2 + lz;
+        if (in_grid(gx, gy, gz, dims)) {
+          size_t gi = 4 * ((size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz));
+          atomicAdd(&grid[gi], mx);
+          atomicAdd(&grid[gi + 1], my);
+          atomicAdd(&grid[gi + 2], mz);
+          atomicAdd(&grid[gi + 3], m);
+        }
+      }
+    }
+    __syncthreads();   // the tile is reused by the next chunk
+  }
+}
+
+// ------------------------------------------------------------------ P2G kernel (mpm.js:306-401)
+template <int PPT>
+__global__ void __launch_bounds__(kCtaThreads) k_p2g(TickInfo t) {
+  extern __shared__ int smem[];
+  int* tile = smem;
+  int* sbox = smem + 4 * t.tile_nodes;
+  for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, chunk)];
+    const uint32_t flags = ts.flags;
+    if (!(flags & F_P2G)) continue;
+    const SceneParams* prm = ts.prm;
+    const int first = (int)(chunk - ts.pchunk_begin) * (kCtaThreads * PPT);
+    const int32_t dims[3] = {prm->dims[0], prm->dims[1], prm->dims[2]};
+    const float4* src = ts.P;
+    const int64_t cap = ts.cap;
+    Scat s[PPT];
+    bool valid[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+      const int i = first + k * kCtaThreads + threadIdx.x;
+      valid[k] = i < ts.n;
+      if (valid[k]) {
+        float4 x = __ldg(&src[i]), v = __ldg(&src[cap + i]);
+        float4 c0 = __ldg(&src[2 * cap + i]), c1 = __ldg(&src[3 * cap + i]), c2 = __ldg(&src[4 * cap + i]);
+        float t01 = __ldg(&src[5 * cap + i].w), t02 = __ldg(&src[6 * cap + i].w), t12 = __ldg(&src[7 * cap + i].w);
+        prep_scatter(s[k], x, v, c0, c1, c2, t01, t02, t12, prm);
+      }
+    }
+    cta_scatter<PPT>(s, valid, dims, reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0,
+                     t.tile_nodes, tile, sbox);
+  }
+}
+
+// zero the grid of scenes whose P2G target is not known to be clear (p2g() clears first, mpm.js:609)
+__global__ void __launch_bounds__(kCtaThreads) k_clear(TickInfo t) {
+  for (uint32_t chunk = blockIdx.x; chunk < t.nchunks; chunk += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_n(t.ts, t.nscenes, chunk)];
+    if (!(ts.flags & F_CLEAR)) continue;
+    const SceneParams* prm = ts.prm;
+    const int64_t nodes = (int64_t)prm->dims[0] * prm->dims[1] * prm->dims[2];
+    const int64_t first = (int64_t)(chunk - ts.nchunk_begin) * kNodeChunk;
+    const int64_t last = min(first + (int64_t)kNodeChunk, nodes);
+    for (int64_t i = first + threadIdx.x; i < last; i += blockDim.x) ts.grid[i] = make_int4(0, 0, 0, 0);
+  }
+}
+
+// the reorder of _sort() on its own (mpm.js:572-577): Palt[i] = P[perm[i]]
+__global__ void __launch_bounds__(kCtaThreads) k_reorder(TickInfo t, const uint32_t* __restrict__ perm) {
+  for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, chunk)];
+    if (!(ts.flags & F_GATHER)) continue;
+    const int first = (int)(chunk - ts.pchunk_begin) * t.chunk;
+    const int last = min(first + t.chunk, ts.n);
+    const int64_t cap = ts.cap;
+    for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+      const int64_t j = __ldg(&perm[ts.seg_base + i]);
+#pragma unroll
+      for (int k = 0; k < kStreams; k++) ts.Palt[k * cap + i] = __ldg(&ts.P[k * cap + j]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ grid update (mpm.js:414-471)
+__device__ __forceinline__ float collider_sdf(uint32_t kind, v3 d, float4 s) {
+  if (kind == 0u) return vlen(d) - s.x;
+  if (kind == 1u) {
+    v3 q = V(fabsf(d.x) - s.x, fabsf(d.y) - s.y, fabsf(d.z) - s.z);
+    v3 qm = V(fmaxf(q.x, 0.0f), fmaxf(q.y, 0.0f), fmaxf(q.z, 0.0f));
+    return vlen(qm) + fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.0f);
+  }
+  return vdot(d, V(s.x, s.y, s.z));
+}
+
+__global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
+  for (uint32_t chunk = blockIdx.x; chunk < t.nchunks; chunk += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_n(t.ts, t.nscenes, chunk)];
+    const SceneParams* prm = ts.prm;
+    const int64_t X = prm->dims[0], Y = prm->dims[1];
+    const int64_t nodes = X * Y * prm->dims[2];
+    const int64_t first = (int64_t)(chunk - ts.nchunk_begin) * kNodeChunk;
+    const int64_t last = min(first + (int64_t)kNodeChunk, nodes);
+    const float bound = prm->bound, ff = prm->floor_friction;
+    const float g0 = prm->gravity[0], g1 = prm->gravity[1], g2 = prm->gravity[2];
+    const v3 hi = V((float)prm->dims[0] - bound, (float)prm->dims[1] - bound, (float)prm->dims[2] - bound);
+    const int ncol = prm->ncol;
+    const bool clear_next = !(ts.flags & F_NO_CLEAR_NEXT);
+    for (int64_t i = first + threadIdx.x; i < last; i += blockDim.x) {
+      int4 g = ts.grid[i];
+      float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (g.w > 0) {
+        const float inv = 1.0f / 4194304.0f;
+        float m = (float)g.w * inv;
+        v3 v = V(((float)g.x * inv) / m + g0, ((float)g.y * inv) / m + g1, ((float)g.z * inv) / m + g2);
+        v3 c = V((float)(i % X), (float)((i / X) % Y), (float)(i / (X * Y)));
+        if (c.y < bound && v.y < 0.0f) {
+          float vn = -v.y;
+          v.y = 0.0f;
+          float vt = sqrtf(v.x * v.x + v.z * v.z);
+          if (vt > 1e-9f) {
+            float f = fmaxf(0.0f, 1.0f - (ff * vn) / vt);
+            v = V(v.x * f, 0.0f, v.z * f);
+          }
+        }
+        if (c.x < bound && v.x < 0.0f) v.x = 0.0f;
+        if (c.z < bound && v.z < 0.0f) v.z = 0.0f;
+        if (c.x > hi.x && v.x > 0.0f) v.x = 0.0f;
+        if (c.y > hi.y && v.y > 0.0f) v.y = 0.0f;
+        if (c.z > hi.z && v.z > 0.0f) v.z = 0.0f;
+        for (int k = 0; k < ncol; k++) {
+          const float4 h = prm->cols[3 * k], s = prm->cols[3 * k + 1], cvv = prm->cols[3 * k + 2];
+          const v3 cv = V(cvv.x, cvv.y, cvv.z);
+          const uint32_t kind = __float_as_uint(h.x);
+          const v3 d = V(c.x - h.y, c.y - h.z, c.z - h.w);
+          float dist = collider_sdf(kind, d, s);
+          if (dist < 1.0f) {
+            const float e = 0.5f;
+            v3 nr = V(collider_sdf(kind, V(d.x + e, d.y, d.z), s) - collider_sdf(kind, V(d.x - e, d.y, d.z), s),
+                      collider_sdf(kind, V(d.x, d.y + e, d.z), s) - collider_sdf(kind, V(d.x, d.y - e, d.z), s),
+                      collider_sdf(kind, V(d.x, d.y, d.z + e), s) - collider_sdf(kind, V(d.x, d.y, d.z - e), s));
+            nr = V(nr.x + 0.0f, nr.y + 1e-7f, nr.z + 0.0f);
+            float ln = vlen(nr);
+            nr = V(nr.x / ln, nr.y / ln, nr.z / ln);
+            v3 vr = vsub(v, cv);
+            float vn = vdot(vr, nr);
+            if (vn < 0.0f) {
+              vr = vsub(vr, vscale(vn, nr));
+              float vt = vlen(vr);
+              if (vt > 1e-9f) vr = vscale(fmaxf(0.0f, 1.0f - (s.w * -vn) / vt), vr);
+              v = vadd(vr, cv);
+            }
+          }
+        }
+        out = make_float4(v.x, v.y, v.z, m);
+      }
+      reinterpret_cast<float4*>(ts.grid)[i] = out;
+      if (clear_next) ts.grid_next[i] = make_int4(0, 0, 0, 0);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ G2P (mpm.js:474-560)
+__device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, float4& C1, float4& C2,
+                                             float4& F0, float4& F1, float4& F2, const SceneParams* prm,
+                                             const float4* __restrict__ grid) {
+  const int32_t dx0 = prm->dims[0], dx1 = prm->dims[1], dx2 = prm->dims[2];
+  const int b0 = base_of(X.x, dx0), b1 = base_of(X.y, dx1), b2 = base_of(X.z, dx2);
+  const float f0 = X.x - (float)b0, f1 = X.y - (float)b1, f2 = X.z - (float)b2;
+  float wx[3], wy[3], wz[3];
+  bspline(f0, wx); bspline(f1, wy); bspline(f2, wz);
+  v3 v = V(0.0f, 0.0f, 0.0f);
+  m3 B;
+  B.c[0] = V(0.0f, 0.0f, 0.0f); B.c[1] = V(0.0f, 0.0f, 0.0f); B.c[2] = V(0.0f, 0.0f, 0.0f);
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float dpx = (float)a - f0;
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+      const float dpy = (float)b - f1;
+      const float wab = wx[a] * wy[b];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const float dpz = (float)c - f2;
+        const float wt = wab * wz[c];
+        const int gx = b0 + a, gy = b1 + b, gz = b2 + c;
+        v3 gv = V(0.0f, 0.0f, 0.0f);
+        if ((unsigned)gx < (unsigned)dx0 && (unsigned)gy < (unsigned)dx1 && (unsigned)gz < (unsigned)dx2) {
+          const float4 n = __ldg(&grid[(size_t)gx + (size_t)dx0 * ((size_t)gy + (size_t)dx1 * (size_t)gz)]);
+          gv = V(n.x, n.y, n.z);
+        }
+        const v3 t = vscale(wt, gv);
+        v = vadd(v, t);
+        B.c[0] = vadd(B.c[0], vscale(dpx, t));
+        B.c[1] = vadd(B.c[1], vscale(dpy, t));
+        B.c[2] = vadd(B.c[2], vscale(dpz, t));
+      }
+    }
+  }
+  m3 C;
+  C.c[0] = vscale(4.0f, B.c[0]); C.c[1] = vscale(4.0f, B.c[1]); C.c[2] = vscale(4.0f, B.c[2]);
+  const float sp = vlen(v);
+  if (sp > prm->vmax) v = vscale(prm->vmax / sp, v);
+  const float bound = prm->bound;
+  const float lo = bound - 1.0f;
+  const float nx = clampf(X.x + v.x, lo, ((float)dx0 - bound) + 1.0f);
+  const float ny = clampf(X.y + v.y, lo, ((float)dx1 - bound) + 1.0f);
+  const float nz = clampf(X.z + v.z, lo, ((float)dx2 - bound) + 1.0f);
+  const uint32_t mid = __float_as_uint(X.w) & 7u;
+  const float4 m0 = prm->mats[mid * 3], m1 = prm->mats[mid * 3 + 1], m2 = prm->mats[mid * 3 + 2];
+  const uint32_t kind = __float_as_uint(m0.x);
+  m3 F;
+  F.c[0] = V(F0.x, F0.y, F0.z); F.c[1] = V(F1.x, F1.y, F1.z); F.c[2] = V(F2.x, F2.y, F2.z);
+  float t00, t11, t22, t01, t02, t12;   // tau[0].x tau[1].y tau[2].z tau[1].x tau[2].x tau[2].y
+  float vw = Vv.w;
+  if (kind == 0u) {
+    const float J = clampf(vw * (1.0f + ((C.c[0].x + C.c[1].y) + C.c[2].z)), 0.6f, 1.4f);
+    vw = J;
+    const float a = m0.z * fminf(J - 1.0f, 0.02f);
+    const float b = m1.x * J;
+    t00 = a * 1.0f + b * (C.c[0].x + C.c[0].x);
+    t11 = a * 1.0f + b * (C.c[1].y + C.c[1].y);
+    t22 = a * 1.0f + b * (C.c[2].z + C.c[2].z);
+    t01 = a * 0.0f + b * (C.c[1].x + C.c[0].y);
+    t02 = a * 0.0f + b * (C.c[2].x + C.c[0].z);
+    t12 = a * 0.0f + b * (C.c[2].y + C.c[1].z);
+    F.c[0] = V(1.0f, 0.0f, 0.0f); F.c[1] = V(0.0f, 1.0f, 0.0f); F.c[2] = V(0.0f, 0.0f, 1.0f);
+  } else {
+    m3 IC;
+    IC.c[0] = V(1.0f + C.c[0].x, 0.0f + C.c[0].y, 0.0f + C.c[0].z);
+    IC.c[1] = V(0.0f + C.c[1].x, 1.0f + C.c[1].y, 0.0f + C.c[1].z);
+    IC.c[2] = V(0.0f + C.c[2].x, 0.0f + C.c[2].y, 1.0f + C.c[2].z);
+    F = mm(IC, F);
+    const float mu0 = m0.z, la0 = m0.w;
+    if (kind == 1u) {
+      const float J = fmaxf(det3(F), 0.05f);
+      const m3 FFt = mm(F, mT(F));
+      const float l = la0 * si_logf(J);
+      t00 = mu0 * (FFt.c[0].x - 1.0f) + l * 1.0f;
+      t11 = mu0 * (FFt.c[1].y - 1.0f) + l * 1.0f;
+      t22 = mu0 * (FFt.c[2].z - 1.0f) + l * 1.0f;
+      t01 = mu0 * (FFt.c[1].x - 0.0f) + l * 0.0f;
+      t02 = mu0 * (FFt.c[2].x - 0.0f) + l * 0.0f;
+      t12 = mu0 * (FFt.c[2].y - 0.0f) + l * 0.0f;
+    } else if (kind == 2u) {
+      m3 U, Vm; v3 sv;
+      svd3(F, U, sv, Vm);
+      const float lo_s = 1.0f - m1.z, hi_s = 1.0f + m1.w;
+      const v3 s = V(clampf(sv.x, lo_s, hi_s), clampf(sv.y, lo_s, hi_s), clampf(sv.z, lo_s, hi_s));
+      const float Jold = (sv.x * sv.y) * sv.z;
+      const float Jnew = (s.x * s.y) * s.z;
+      vw = clampf((vw * Jold) / Jnew, 0.6f, 20.0f);
+      F = mm(mdiag_right(U, s), mT(Vm));
+      const float h = si_expf(m1.y * (1.0f - vw));
+      const float mu = mu0 * h, la = la0 * h;
+      const m3 R = mm(U, mT(Vm));
+      const float J = Jnew;
+      const float tm = 2.0f * mu;
+      m3 FR;
+      FR.c[0] = vscale(tm, vsub(F.c[0], R.c[0]));
+      FR.c[1] = vscale(tm, vsub(F.c[1], R.c[1]));
+      FR.c[2] = vscale(tm, vsub(F.c[2], R.c[2]));
+      const m3 P1 = mm(FR, mT(F));
+      const float l = (la * J) * (J - 1.0f);
+      t00 = P1.c[0].x + l * 1.0f;
+      t11 = P1.c[1].y + l * 1.0f;
+      t22 = P1.c[2].z + l * 1.0f;
+      t01 = P1.c[1].x + l * 0.0f;
+      t02 = P1.c[2].x + l * 0.0f;
+      t12 = P1.c[2].y + l * 0.0f;
+    } else {
+      m3 U, Vm; v3 sv;
+      svd3(F, U, sv, Vm);
+      v3 e = V(si_logf(fmaxf(fabsf(sv.x), 1e-4f)), si_logf(fmaxf(fabsf(sv.y), 1e-4f)),
+               si_logf(fmaxf(fabsf(sv.z), 1e-4f)));
+      const float tr = (e.x + e.y) + e.z;
+      const float tr3 = tr / 3.0f;
+      const v3 dev = V(e.x - tr3, e.y - tr3, e.z - tr3);
+      const float devn = vlen(dev);
+      if (tr >= 0.0f) {
+        e = V(0.0f, 0.0f, 0.0f);
+      } else {
+        const float dg = devn + (((3.0f * la0 + 2.0f * mu0) / (2.0f * mu0)) * tr) * m2.x;
+        if (dg > 0.0f && devn > 1e-12f)
+          e = V(e.x - (dg * dev.x) / devn, e.y - (dg * dev.y) / devn, e.z - (dg * dev.z) / devn);
+      }
+      const v3 s = V(si_expf(e.x), si_expf(e.y), si_expf(e.z));
+      F = mm(mdiag_right(U, s), mT(Vm));
+      const float te = (e.x + e.y) + e.z;
+      const float tm = 2.0f * mu0;
+      const float lt = la0 * te;
+      const v3 dd = V(tm * e.x + lt, tm * e.y + lt, tm * e.z + lt);
+      const m3 T = mm(mdiag_right(U, dd), mT(U));
+      t00 = T.c[0].x; t11 = T.c[1].y; t22 = T.c[2].z;
+      t01 = T.c[1].x; t02 = T.c[2].x; t12 = T.c[2].y;
+    }
+  }
+  X = make_float4(nx, ny, nz, X.w);
+  Vv = make_float4(v.x, v.y, v.z, vw);
+  C0 = make_float4(C.c[0].x, C.c[0].y, C.c[0].z, t00);
+  C1 = make_float4(C.c[1].x, C.c[1].y, C.c[1].z, t11);
+  C2 = make_float4(C.c[2].x, C.c[2].y, C.c[2].z, t22);
+  F0 = make_float4(F.c[0].x, F.c[0].y, F.c[0].z, t01);
+  F1 = make_float4(F.c[1].x, F.c[1].y, F.c[1].z, t02);
+  F2 = make_float4(F.c[2].x, F.c[2].y, F.c[2].z, t12);
+}
+
+template <int PPT>
+__global__ void __launch_bounds__(kCtaThreads) k_g2p(TickInfo t, const uint32_t* __restrict__ perm) {
+  extern __shared__ int smem[];
+  int* tile = smem;
+  int* sbox = smem + 4 * t.tile_nodes;
+  for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, chunk)];
+    const uint32_t flags = ts.flags;
+    const SceneParams* prm = ts.prm;
+    const int first = (int)(chunk - ts.pchunk_begin) * (kCtaThreads * PPT);
+    const bool fuse = (flags & F_FUSE) != 0;
+    const bool gather = (flags & F_GATHER) != 0;
+    const float4* Pin = ts.P;
+    float4* P = gather ? ts.Palt : ts.P;
+    const int64_t cap = ts.cap;
+    const float4* grid = reinterpret_cast<const float4*>(ts.grid);
+    Scat s[PPT];
+    bool valid[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+      const int i = first + k * kCtaThreads + threadIdx.x;
+      valid[k] = i < ts.n;
+      if (valid[k]) {
+        const int64_t j = gather ? (int64_t)__ldg(&perm[ts.seg_base + i]) : (int64_t)i;
+        float4 x = Pin[j], v = Pin[cap + j], c0 = Pin[2 * cap + j], c1 = Pin[3 * cap + j], c2 = Pin[4 * cap + j];
+        float4 f0 = Pin[5 * cap + j], f1 = Pin[6 * cap + j], f2 = Pin[7 * cap + j];
+        g2p_particle(x, v, c0, c1, c2, f0, f1, f2, prm, grid);
+        P[i] = x; P[cap + i] = v; P[2 * cap + i] = c0; P[3 * cap + i] = c1; P[4 * cap + i] = c2;
+        P[5 * cap + i] = f0; P[6 * cap + i] = f1; P[7 * cap + i] = f2;
+        if (flags & F_KEYS) ts.keys[i] = block_key(x.x, x.y, x.z, prm->num_blocks);
+        if (fuse) prep_scatter(s[k], x, v, c0, c1, c2, f0.w, f1.w, f2.w, prm);
+      }
+    }
+    if (fuse) {
+      const int32_t dims[3] = {prm->dims[0], prm->dims[1], prm->dims[2]};
+      cta_scatter<PPT>(s, valid, dims, reinterpret_cast<int*>(ts.grid_next), false, t.tile_nodes, tile, sbox);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ keys of the current positions
+__global__ void __launch_bounds__(kCtaThreads) k_keys(TickInfo t) {
+  const int per = kCtaThreads * (t.chunk / kCtaThreads);
+  for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, chunk)];
+    if (!(ts.flags & F_KEYS_NOW)) continue;
+    const int first = (int)(chunk - ts.pchunk_begin) * per;
+    const int last = min(first + per, ts.n);
+    const uint32_t nb = ts.prm->num_blocks;
+    for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+      float4 x = ts.P[i];
+      ts.keys[i] = block_key(x.x, x.y, x.z, nb);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ retime (mpm.js:405-413)
+__global__ void k_retime(float4* P, int64_t cap, int32_t n, float k) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int r = 1; r <= 4; r++) {
+      float4 a = P[r * cap + i];
+      P[r * cap + i] = make_float4(a.x * k, a.y * k, a.z * k, a.w);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ record I/O
+__global__ void k_aos_to_soa(const float4* __restrict__ aos, float4* P, int64_t cap, int64_t off, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * kStreams; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = t / kStreams; int k = (int)(t % kStreams);
+    P[k * cap + off + i] = aos[t];
+  }
+}
+__global__ void k_soa_to_aos(const float4* __restrict__ P, int64_t cap, int64_t off, int64_t n, float4* aos) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * kStreams; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = t / kStreams; int k = (int)(t % kStreams);
+    aos[t] = P[k * cap + off + i];
+  }
+}
+// readPositions, mpm.js:627-628: f32(x * dx + origin) evaluated in f64 like JavaScript
+__global__ void k_positions(const float4* __restrict__ P, int64_t off, int64_t n, double dx, double o0,
+                            double o1, double o2, float* xyz) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float4 x = P[off + i];
+    xyz[3 * i] = (float)(__dadd_rn(__dmul_rn((double)x.x, dx), o0));
+    xyz[3 * i + 1] = (float)(__dadd_rn(__dmul_rn((double)x.y, dx), o1));
+    xyz[3 * i + 2] = (float)(__dadd_rn(__dmul_rn((double)x.z, dx), o2));
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+int p2g_smem_bytes(int tile_nodes) { return tile_nodes * 16 + 32; }
+
+template <int PPT>
+static void set_smem_attr(int tile_nodes) {
+  int bytes = p2g_smem_bytes(tile_nodes);
+  if (bytes > 48 * 1024) {
+    cudaFuncSetAttribute(k_p2g<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_g2p<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
+}
+
+void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st) {
+  if (t.pchunks == 0) return;
+  int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
+  int smem = p2g_smem_bytes(t.tile_nodes);
+  switch (t.chunk / kCtaThreads) {
+    case 1: k_p2g<1><<<ctas, kCtaThreads, smem, st>>>(t); break;
+    case 4: k_p2g<4><<<ctas, kCtaThreads, smem, st>>>(t); break;
+    default: k_p2g<2><<<ctas, kCtaThreads, smem, st>>>(t); break;
+  }
+}
+void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st) {
+  if (t.pchunks == 0) return;
+  int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
+  int smem = p2g_smem_bytes(t.tile_nodes);
+  switch (t.chunk / kCtaThreads) {
+    case 1: k_g2p<1><<<ctas, kCtaThreads, smem, st>>>(t, perm); break;
+    case 4: k_g2p<4><<<ctas, kCtaThreads, smem, st>>>(t, perm); break;
+    default: k_g2p<2><<<ctas, kCtaThreads, smem, st>>>(t, perm); break;
+  }
+}
+void launch_clear(const TickInfo& t, int grid_ctas, cudaStream_t st) {
+  if (t.nchunks == 0) return;
+  int ctas = (int)std::min<uint32_t>(t.nchunks, (uint32_t)grid_ctas);
+  k_clear<<<ctas, kCtaThreads, 0, st>>>(t);
+}
+void launch_reorder(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st) {
+  if (t.pchunks == 0) return;
+  int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
+  k_reorder<<<ctas, kCtaThreads, 0, st>>>(t, perm);
+}
+void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st) {
+  if (t.nchunks == 0) return;
+  int ctas = (int)std::min<uint32_t>(t.nchunks, (uint32_t)grid_ctas);
+  k_grid<<<ctas, kCtaThreads, 0, st>>>(t);
+}
+void launch_keys(const TickInfo& t, int grid_ctas, cudaStream_t st) {
+  if (t.pchunks == 0) return;
+  int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
+  k_keys<<<ctas, kCtaThreads, 0, st>>>(t);
+}
+void launch_retime(float4* P, int64_t cap, int32_t n, float k, cudaStream_t st) {
+  if (n <= 0) return;
+  int ctas = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  k_retime<<<ctas, 256, 0, st>>>(P, cap, n, k);
+}
+void launch_aos_to_soa(const float* aos, float4* P, int64_t cap, int64_t off, int64_t n, cudaStream_t st) {
+  if (n <= 0) return;
+  int ctas = (int)std::min<int64_t>((n * kStreams + 255) / 256, 8192);
+  k_aos_to_soa<<<ctas, 256, 0, st>>>(reinterpret_cast<const float4*>(aos), P, cap, off, n);
+}
+void launch_soa_to_aos(const float4* P, int64_t cap, int64_t off, int64_t n, float* aos, cudaStream_t st) {
+  if (n <= 0) return;
+  int ctas = (int)std::min<int64_t>((n * kStreams + 255) / 256, 8192);
+  k_soa_to_aos<<<ctas, 256, 0, st>>>(P, cap, off, n, reinterpret_cast<float4*>(aos));
+}
+void launch_positions(const float4* P, int64_t cap, int64_t off, int64_t n, double dx, const double origin[3],
+                      float* xyz, cudaStream_t st) {
+  (void)cap;
+  if (n <= 0) return;
+  int ctas = (int)std::min<int64_t>((n + 255) / 256, 8192);
+  k_positions<<<ctas, 256, 0, st>>>(P, off, n, dx, origin[0], origin[1], origin[2], xyz);
+}
+
+void configure_kernels(int tile_nodes) {
+  set_smem_attr<1>(tile_nodes);
+  set_smem_attr<2>(tile_nodes);
+  set_smem_attr<4>(tile_nodes);
+}
+
+int occupancy_ctas(int which, int tile_nodes) {
+  int n = 0;
+  int smem = p2g_smem_bytes(tile_nodes);
+  switch (which) {
+    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<2>, kCtaThreads, smem); break;
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<2>, kCtaThreads, smem); break;
+    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_grid, kCtaThreads, 0); break;
+    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<1>, kCtaThreads, smem); break;
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<4>, kCtaThreads, smem); break;
+    default: break;
+  }
+  return n > 0 ? n : 1;
+}
+
+}  // namespace si

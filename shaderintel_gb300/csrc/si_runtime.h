@@ -1,0 +1,107 @@
+// si_runtime.h — host objects of libsi_cuda (internal): the world, the scene, cached graph plans.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "si_cuda.h"
+#include "si_device.h"
+
+struct GraphTick {
+  int mode;
+  uint32_t pchunks, nchunks;
+  bool any_p2g, any_clear, any_gather, any_keys_now;
+  uint32_t sort_n;
+  int passes;
+};
+
+// A plan of ticks captured once and replayed while the tables it was built from repeat.
+struct GraphPlan {
+  cudaGraphExec_t exec = nullptr;
+  void* table = nullptr;            // device copy of the plan's tick tables
+  std::vector<uint8_t> bytes;       // host copy, the replay key
+  std::vector<GraphTick> ticks;
+  int ppt = 0, tile_nodes = 0;
+  uint64_t last_use = 0;
+  int64_t kernels = 0;              // kernels in the graph
+  ~GraphPlan();
+};
+
+struct si_world {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  int sms = 1;
+  int max_smem_optin = 48 * 1024;
+  std::vector<si_mpm*> scenes;
+  bool destroyed = false;
+  std::atomic<si_server*> server{nullptr};
+  std::recursive_mutex api_mu;      // serialises API calls on this world with the server's rounds
+  // tuning (autotuner: particles per CTA = 256 * ppt, shared tile capacity in nodes)
+  int ppt = 2, tile_nodes = 1024;
+  int ctas_p2g = 0, ctas_g2p = 0, ctas_grid = 0, ctas_misc = 0;
+  // sort scratch (grown on demand)
+  uint32_t *ka = nullptr, *va = nullptr, *kb = nullptr, *vb = nullptr;
+  size_t sort_cap = 0;
+  uint32_t* hist = nullptr;
+  size_t hist_cap = 0;
+  uint32_t* digit_total = nullptr;
+  // tick tables of direct (non-graph) execution
+  si::TickScene* tab = nullptr;
+  size_t tab_cap = 0;
+  // graphs
+  bool use_graphs = true;
+  std::vector<std::unique_ptr<GraphPlan>> graphs;
+  uint64_t graph_clock = 0;
+  // profiling: per-phase time [sort, p2g, grid, g2p]
+  bool profile = false;
+  double prof_ms[4] = {0, 0, 0, 0};
+  cudaEvent_t pev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t marks[8] = {};
+  int64_t launches = 0;             // kernels enqueued (graph replays add their kernel count)
+};
+
+struct si_mpm {
+  si_world* w = nullptr;
+  bool own_world = false;
+  bool destroyed = false;
+  // properties of the reference object (mpm.js:89-127)
+  int64_t cap = 0;                  // maxParticles
+  int32_t dims[3] = {0, 0, 0};
+  double dx = 0, size[3] = {0, 0, 0}, origin[3] = {0, 0, 0}, gravity[3] = {0, 0, 0};
+  int32_t substeps = 8, sort_every = 4, ppc_axis = 2, bound = 3;
+  double time_scale = 1, dt = 0;
+  int64_t count = 0, step_count = 0, nodes = 0;
+  uint32_t num_blocks = 0;
+  float mats[96] = {};
+  int32_t nmats = 0;
+  float cols[192] = {};
+  int32_t ncol = 0;
+  // device state
+  float4* pbuf[2] = {nullptr, nullptr};
+  int pcur = 0;
+  int4* grid[2] = {nullptr, nullptr};
+  int gcur = 0;                     // grid of the last substep
+  uint32_t* keys = nullptr;
+  uint32_t* starts = nullptr;
+  si::SceneParams* prm = nullptr;
+  bool prm_dirty = true;
+  bool pending = false;             // grid[1-gcur] holds the P2G of the current particle state
+  bool next_clear = false;          // grid[1-gcur] is zero
+  bool keys_valid = false;          // keys hold the block keys of the current positions
+  int64_t device_bytes = 0;
+  // serving: a scene admitted by a server is retired through it
+  bool served = false;
+};
+
+int world_configure(si_world* w, int ppt, int tile_nodes);
+int run_substeps(si_world* w, const std::vector<si_mpm*>& scenes, int K);
+int scene_create(si_world* w, const si_mpm_desc* in, si_mpm** out, bool own_world);
+int64_t scene_footprint_of(const si_mpm_desc* in);
+
+namespace si {
+void configure_kernels(int tile_nodes);
+}

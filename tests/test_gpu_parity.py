@@ -1,0 +1,279 @@
+"""GPU parity: the CUDA substep through the C ABI against the CPU oracle, from identical state.
+
+Bar: keys, counts/starts and grid i32 sums bit-exact; grid update and particle state bit-exact
+as well (the kernels follow the oracle's f32 order), checked against the stated tolerance of
+1e-5 max relative error first so a failure reports its size. The reference's own MPM tests
+(tests/physics.test.js:6-59, tests/lifecycle.test.js:231-307) are restated at the end."""
+import numpy as np
+import pytest
+
+import host_ref
+import si_oracle as O
+from conftest import mulberry32
+from shaderintel_gb300 import MPM, SIError, World
+
+pytestmark = pytest.mark.gpu
+REL_TOL = 1e-5   # particle-state tolerance per substep (stated by the hot-path contract)
+
+
+def tables(sim):
+    mats = np.zeros((8, 12), np.float32)
+    rows = getattr(sim, "_rows", [])
+    if rows:
+        mats[:len(rows)] = np.stack(rows)
+    cols = np.zeros((16, 12), np.float32)
+    cr = sim._collider_rows()
+    if len(cr):
+        cols[:len(cr)] = cr
+    dt = sim.substepDt
+    grav = [np.float32((g * dt * dt) / sim.dx) for g in sim.gravity]
+    vol4 = np.float32(4 * (1 / sim.ppcAxis ** 3))
+    return mats, cols, len(cr), grav, vol4
+
+
+def rel_err(a, b):
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(1.0, np.abs(b)))) if a.size else 0.0
+
+
+def assert_records_equal(got, want):
+    assert got.shape == want.shape
+    fin = np.isfinite(want)
+    assert np.array_equal(np.isfinite(got), fin)
+    assert rel_err(got[fin], want[fin]) <= REL_TOL
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
+        f"{int((got.view(np.uint32) != want.view(np.uint32)).sum())} words differ"
+
+
+def randomise(rec, seed=3):
+    R = mulberry32(seed)
+    for k in range(len(rec)):
+        for a in range(3):
+            rec[k, 4 + a] = (R() - 0.5) * 0.4
+        for c in range(3):
+            for a in range(3):
+                rec[k, 8 + 4 * c + a] = (R() - 0.5) * 0.2
+        for o in (11, 15, 19, 23, 27, 31):
+            rec[k, o] = (R() - 0.5) * 0.3
+    return rec
+
+
+def mixed_scene(grid=32, maxp=120000, **kw):
+    sim = MPM(grid=grid, maxParticles=maxp, **kw)
+    sim.add({"box": [[0.1, 0.1, 0.1], [0.45, 0.5, 0.9]]}, material="water")
+    sim.add({"sphere": [[0.7, 0.55, 0.35], 0.12]}, material="jelly", velocity=[0, -1, 0])
+    sim.add({"box": [[0.6, 0.1, 0.6], [0.85, 0.3, 0.85]]}, material="snow")
+    sim.add({"cylinder": [[0.7, 0.6, 0.75], 0.08, 0.1]}, material="sand", velocity=[-0.5, 0, 0])
+    sim.add({"sphere": [[0.3, 0.75, 0.5], 0.08]}, material="honey")
+    return sim
+
+
+def test_records_and_colliders_match_reference_host_math():
+    sim = MPM(grid=40, maxParticles=50000, substeps=6, origin=[0.1, -0.2, 0.3])
+    shape = {"sphere": [[0.5, 0.3, 0.7], 0.15]}
+    n = sim.add(shape, material="rubber", velocity=[0.3, -1.2, 0.05], seed=5)
+    rec = sim.readParticles()
+    pts = host_ref.sample_shape(shape, sim.dx / 2, 0.6, 5)
+    want = host_ref.make_records(pts, 0, [0.3, -1.2, 0.05], sim.dims, sim.dx, sim.origin, sim.substepDt)
+    assert n == len(want)
+    assert np.array_equal(rec.view(np.uint32), want.view(np.uint32))
+    cols = [{"type": "sphere", "center": [0.5, 0.5, 0.5], "radius": 0.1, "velocity": [0, 1, 0]},
+            {"type": "box", "center": [0.3, 0.2, 0.1], "half": [0.1, 0.05, 0.2], "friction": 0.6},
+            {"type": "plane", "center": [0, 0.1, 0], "normal": [0, 1, 0]}]
+    sim.setColliders(cols)
+    got = sim._collider_rows()
+    for g, c in zip(got, cols):
+        w = host_ref.collider_row(c, sim.dx, sim.origin, sim.substepDt)
+        assert np.array_equal(g.view(np.uint32), w.view(np.uint32))
+    sim.destroy()
+
+
+@pytest.mark.parametrize("force_global", [False, True])
+def test_p2g_bit_exact_and_conserving(force_global):
+    """tests/physics.test.js:6-32 + bit-exact grid against the oracle, tile and global paths."""
+    sim = MPM(grid=48, maxParticles=60000, substeps=4)
+    sim.add({"box": [[0.2, 0.2, 0.2], [0.7, 0.6, 0.7]]}, material="water")
+    rec = randomise(sim.readParticles())
+    sim.writeParticles(rec)
+    sim.p2g(forceGlobal=force_global)
+    g = sim.readGrid()
+    mats, _, _, _, vol4 = tables(sim)
+    want = O.p2g(rec, sim.dims, mats, vol4, threads=8)
+    assert np.array_equal(g, want), f"{int((g != want).sum())} grid words differ"
+    FP = 2.0 ** 22
+    pm = len(rec) / 8
+    pp = rec[:, 4:7].astype(np.float64).sum(0) / 8
+    gm = g[:, 3].astype(np.int64).sum() / FP
+    gp = g[:, :3].astype(np.int64).sum(0) / FP
+    assert abs(gm - pm) / pm < 1e-4
+    assert np.abs(gp - pp).max() < 1e-3 * max(1, np.linalg.norm(pp)) + len(rec) * 27 * 4 / FP
+    sim.destroy()
+
+
+def test_tiled_p2g_equals_global_after_steps():
+    """tests/physics.test.js:33-42: tiled == global-atomic P2G, word for word."""
+    sim = MPM(grid=48, maxParticles=80000, substeps=4)
+    sim.add({"box": [[0.1, 0.1, 0.1], [0.9, 0.4, 0.9]]}, material="water")
+    for _ in range(3):
+        sim.step()
+    sim._sort()
+    sim.p2g(forceGlobal=True)
+    a = sim.readGrid()
+    sim.p2g(forceGlobal=False)
+    b = sim.readGrid()
+    assert np.array_equal(a, b)
+    assert a[:, 3].astype(np.int64).sum() > 0
+    sim.destroy()
+
+
+def test_sort_bins_and_order_bit_exact():
+    sim = mixed_scene()
+    for _ in range(2):
+        sim.step()
+    rec = sim.readParticles()
+    sim._sort()
+    keys, starts = sim.readBins()
+    nb = O.num_blocks(sim.dims)
+    dst, wkeys, wstarts, _ = O.sort(rec, nb)
+    assert np.array_equal(keys, wkeys)
+    assert np.array_equal(starts, wstarts)
+    assert_records_equal(sim.readParticles(), dst)
+    sim.destroy()
+
+
+def test_phases_bit_exact_all_materials():
+    """P2G, grid update (walls, floor friction, three collider kinds) and G2P for water, jelly,
+    snow, sand and honey from identical state."""
+    sim = mixed_scene()
+    sim.setColliders([
+        {"type": "sphere", "center": [0.5, 0.3, 0.5], "radius": 0.1, "velocity": [0.2, 0, 0], "friction": 0.5},
+        {"type": "box", "center": [0.25, 0.15, 0.7], "half": [0.08, 0.05, 0.1]},
+        {"type": "plane", "center": [0, 0.12, 0], "normal": [0.1, 1, 0]}])
+    for _ in range(4):
+        sim.step()
+    mats, cols, ncol, grav, vol4 = tables(sim)
+    rec0 = sim.readParticles()
+    sim.p2g()
+    g = sim.readGrid()
+    wg = O.p2g(rec0, sim.dims, mats, vol4, threads=8)
+    assert np.array_equal(g, wg)
+    sim.gridUpdate()
+    gu = sim.readGrid()
+    wgu = O.grid_update(wg, sim.dims, grav, cols, ncol, threads=8)
+    assert np.array_equal(gu, wgu), f"{int((gu != wgu).sum())} grid words differ after the update"
+    sim.g2p()
+    rec1 = sim.readParticles()
+    want = O.g2p(rec0, sim.dims, wgu, mats, threads=8)
+    kinds = rec0.view(np.uint32)[:, 3]
+    for m in np.unique(kinds):
+        sel = kinds == m
+        assert_records_equal(rec1[sel], want[sel])
+    sim.destroy()
+
+
+@pytest.mark.parametrize("scene", ["dam_break_32", "mixed_32"])
+def test_trajectory_bit_exact(scene):
+    """Whole substeps (sort every 4, fused P2G, graphs) against the oracle's schedule."""
+    if scene == "dam_break_32":
+        # 32^3 grid, 16^3-cell water block at the corner inside the walls: 32,768 particles
+        sim = MPM(grid=32, maxParticles=40000)
+        sim.add({"box": [[3 / 32] * 3, [19 / 32] * 3]}, material="water", seed=1)
+        assert sim.count == 32768
+        K = 200
+    else:
+        sim = mixed_scene()
+        K = 64
+    mats, cols, ncol, grav, vol4 = tables(sim)
+    rec0 = sim.readParticles()
+    sim.step(K=K)
+    got = sim.readParticles()
+    want, wgrid, sc = O.substeps(rec0, sim.dims, mats, cols, ncol, grav, vol4, K, threads=8)
+    assert sim.stepCount == sc == K
+    assert_records_equal(got, want)
+    assert np.array_equal(sim.readGrid(), wgrid)
+    sim.destroy()
+
+
+def test_step_in_pieces_equals_one_call():
+    a = mixed_scene()
+    b = mixed_scene()
+    a.step(K=24)
+    for k in (5, 1, 7, 3, 8):
+        b.step(K=k)
+    assert np.array_equal(a.readParticles().view(np.uint32), b.readParticles().view(np.uint32))
+    a.destroy()
+    b.destroy()
+
+
+def test_dam_break_reference():
+    """tests/physics.test.js:43-59: 48^3, water + jelly, 150 frames."""
+    sim = MPM(grid=48, maxParticles=200000, substeps=8)
+    sim.add({"box": [[0.05, 0.05, 0.05], [0.4, 0.6, 0.95]]}, material="water")
+    sim.add({"sphere": [[0.7, 0.4, 0.5], 0.12]}, material="jelly")
+    for _ in range(150):
+        sim.step()
+    P = sim.readParticles()
+    x = P[:, :3]
+    assert np.isfinite(x).all()
+    assert ((x >= 1) & (x <= np.array(sim.dims) - 1)).all()
+    water = P.view(np.uint32)[:, 3] == 0
+    assert abs(P[water, 7].mean() - 1) < 0.05
+    sim.destroy()
+
+
+def test_retime_keeps_physical_speed():
+    """tests/lifecycle.test.js:294-307."""
+    def speed(substeps):
+        sim = MPM(grid=24, maxParticles=16384, gravity=[0, 0, 0], substeps=8)
+        sim.add({"box": [[0.3, 0.3, 0.3], [0.5, 0.5, 0.5]]}, material="water", velocity=[1, 0, 0])
+        sim.step()
+        sim.substeps = substeps
+        a = sim.readPositions()
+        sim.step()
+        b = sim.readPositions()
+        sim.destroy()
+        return float((b[:, 0] - a[:, 0]).mean() * 60)
+    s8, s16 = speed(8), speed(16)
+    assert abs(s16 / s8 - 1) < 0.05
+
+
+def test_materials_lifecycle_and_validation():
+    """tests/lifecycle.test.js:231-243 and 274-292."""
+    sim = MPM(grid=16, maxParticles=4096)
+    names = ["water", "oil", "honey", "jelly", "rubber", "snow", "sand"]
+    from shaderintel_gb300 import MATERIALS
+    for rnd in range(3):
+        sim.clear()
+        for k in range(7):
+            sim.add({"box": [[0.1, 0.1, 0.1], [0.2, 0.2, 0.2]]},
+                    material=dict(MATERIALS[names[k]], density=1 + rnd * 0.1 + k * 0.01))
+    assert len(sim.materials) == 7 and sim.count > 0
+    sim.step()
+    sim.destroy()
+    sim.destroy()   # idempotent
+    with pytest.raises(SIError):
+        sim.step()
+    sim = MPM(grid=16, maxParticles=8192)
+    sim.add({"box": [[0.3, 0.3, 0.3], [0.6, 0.6, 0.6]]}, material={"kind": "jelly", "poisson": 0.5, "stiffness": 0.5})
+    for _ in range(5):
+        sim.step()
+    assert np.isfinite(sim.readPositions()).all()
+    assert sim.materials[0]["kind"] == 1
+    with pytest.raises(SIError) as e:
+        sim.add({"box": [[0.1, 0.1, 0.1], [0.2, 0.2, 0.2]]}, material={"kind": "fluid", "density": 1000})
+    assert e.value.code == "invalid-argument"
+    sim.destroy()
+
+
+def test_capacity_truncates_add_and_empty_step_is_noop():
+    sim = MPM(grid=16, maxParticles=100)
+    assert sim.count == 0
+    sim.step()                      # count 0: nothing happens (mpm.js:584)
+    assert sim.stepCount == 0
+    n = sim.add({"box": [[0.2, 0.2, 0.2], [0.6, 0.6, 0.6]]})
+    assert n == 100 and sim.count == 100
+    assert sim.add({"box": [[0.2, 0.2, 0.2], [0.3, 0.3, 0.3]]}) == 0
+    sim.step()
+    assert sim.stepCount == sim.substeps
+    sim.destroy()
