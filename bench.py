@@ -134,6 +134,7 @@ def build_cpu(cfg):
 def cpu_measure(cfg, target_s, steps=None, warmup=0):
     """Times the oracle (all host threads) on the scene; returns (particle-substeps/s, substeps, threads)."""
     import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import si_oracle as O
     rec, mats, geo, grav, vol4, _ = build_cpu(cfg)
     threads = os.cpu_count() or 1

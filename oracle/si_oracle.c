@@ -422,9 +422,10 @@ static void g2p_one(float* p, const int32_t dims[3], const int32_t* grid, const 
         }
         v3 t = vscale(wt, gv);
         v = vadd(v, t);
-        B.c[0] = vadd(B.c[0], vscale(dpos.x, t));
-        B.c[1] = vadd(B.c[1], vscale(dpos.y, t));
-        B.c[2] = vadd(B.c[2], vscale(dpos.z, t));
+        /* B += outer3(t, dpos), the one fused multiply-add of the canonical order */
+        B.c[0] = V(fmaf(dpos.x, t.x, B.c[0].x), fmaf(dpos.x, t.y, B.c[0].y), fmaf(dpos.x, t.z, B.c[0].z));
+        B.c[1] = V(fmaf(dpos.y, t.x, B.c[1].x), fmaf(dpos.y, t.y, B.c[1].y), fmaf(dpos.y, t.z, B.c[1].z));
+        B.c[2] = V(fmaf(dpos.z, t.x, B.c[2].x), fmaf(dpos.z, t.y, B.c[2].y), fmaf(dpos.z, t.z, B.c[2].z));
       }
   m3 C;
   for (int j = 0; j < 3; j++) C.c[j] = vscale(4.0f, B.c[j]);

@@ -17,7 +17,9 @@
  *
  * Canonical f32 evaluation order. WGSL pins neither FMA contraction nor the reduction order of
  * matrix products, so this file fixes one order and the CUDA kernels follow it exactly:
- *   - every f32 operation is rounded on its own (no FMA: built with -ffp-contract=off);
+ *   - every f32 operation is rounded on its own (built with -ffp-contract=off), with one exception:
+ *     the G2P gather accumulates B += outer3(wt*gv, dpos) as fmaf(dpos_k, t_i, B_ki) (WGSL lets a
+ *     compiler contract it; P2G, whose i32 sums must match bit for bit, has no fused operation);
  *   - binary expressions evaluate left to right as written in the WGSL;
  *   - mat*vec: r_i = (M0_i*v0 + M1_i*v1) + M2_i*v2 (columns Mk); mat*mat likewise per column;
  *   - dot(a,b) = (a0*b0 + a1*b1) + a2*b2; length = sqrt(dot); normalize(v) = v_i / length(v);

@@ -46,8 +46,17 @@ def _run(cmd):
     return r.stdout
 
 
-def build(force=False, verbose=False):
-    """Compile the CUDA library (if its sources changed) and return its path."""
+def build(force=False, verbose=False, out_dir=None, defines=()):
+    """Compile the CUDA library (if its sources changed) and return its path. out_dir/defines make
+    a variant build (e.g. -DSI_G2P_MIN_CTAS=3) beside the default one."""
+    global OUT, LIB
+    if out_dir is not None:
+        saved = (OUT, LIB)
+        OUT, LIB = out_dir, os.path.join(out_dir, "libsi_cuda.so")
+        try:
+            return build(force, verbose, None, defines)
+        finally:
+            OUT, LIB = saved
     if not force and not _stale():
         return LIB
     if not os.path.exists(NVCC):
@@ -59,7 +68,7 @@ def build(force=False, verbose=False):
         obj = os.path.join(OUT, f + ".o")
         jobs.append(([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
                                       "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                                      "-c", os.path.join(CSRC, f), "-o", obj] + inc, obj))
+                                      "-c", os.path.join(CSRC, f), "-o", obj] + list(defines) + inc, obj))
     cxx = os.environ.get("CXX", "g++")
     for f in CPP_SOURCES:
         obj = os.path.join(OUT, f + ".o")

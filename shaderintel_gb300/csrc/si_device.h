@@ -101,7 +101,8 @@ void launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
 // Per-scene starts (reference blockCount after the scan) of every sorting scene.
 void launch_scene_starts_all(const TickInfo& t, const uint32_t* sorted_keys, uint32_t max_blocks,
                              cudaStream_t st);
-int p2g_smem_bytes(int tile_nodes);
-int occupancy_ctas(int which, int tile_nodes);   // resident CTAs per SM of kernel `which`
+int p2g_smem_bytes(int tile_nodes, int ppt);
+int max_tile_nodes();
+int occupancy_ctas(int which, int tile_nodes, int ppt);   // resident CTAs per SM of kernel `which`
 
 }  // namespace si

@@ -10,7 +10,23 @@
 #include "si_math.cuh"
 #include "si_runtime.h"
 
+// Resident CTAs per SM the G2P/P2G kernels are compiled for (register budget 65536 / (256 * n)).
+#ifndef SI_G2P_MIN_CTAS
+#define SI_G2P_MIN_CTAS 2
+#endif
+
 namespace si {
+
+// Shared tile: kTileNodes nodes, used first as the gather tile of the G2P (vec4f per node) and then
+// as the P2G scatter tile (four planes of i32, stride kTileNodes, so the four channel atomics of a
+// node share one address computation). TickInfo::tile_nodes (<= kTileNodes) is the usable capacity.
+constexpr int kTileNodes = 2048;
+
+// CTA barrier that lanes of one warp may reach along different paths (after an `if` on the lane's
+// own particle or a tail loop). __syncthreads() is the warp-aligned barrier (barrier.sync.aligned),
+// undefined when a warp's lanes arrive at different instructions; the non-aligned form counts each
+// arriving thread, so every thread of the CTA has passed the preceding phase when it completes.
+__device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: "memory"); }
 
 __device__ __forceinline__ int find_scene_p(const TickScene* ts, int n, uint32_t chunk) {
   int lo = 0, hi = n - 1;
@@ -69,12 +85,36 @@ __device__ __forceinline__ bool in_grid(int gx, int gy, int gz, const int32_t* d
   return (unsigned)gx < (unsigned)d[0] && (unsigned)gy < (unsigned)d[1] && (unsigned)gz < (unsigned)d[2];
 }
 
+// i32(round(x * 2^22)) for |x| < 1 in two full-rate instructions: x * 2^22 is exact, so one fused
+// add of 1.5 * 2^23 rounds it to nearest-even exactly like rint, and the low bits of the sum are the
+// integer. Equal to to_fixed(x) wherever it is used (the caller proves |x| < 0.9 first).
+__device__ __forceinline__ int32_t to_fixed_small(float x) {
+  return __float_as_int(__fmaf_rn(x, 4194304.0f, 12582912.0f)) - 0x4B400000;
+}
+
+// True when every value the particle scatters has |x| < 0.9: |wt| <= 1, |dpos| <= 1.5 and
+// |m v_i + affine_i . dpos| <= |m v_i| + 1.5 sum_k |affine_ki| (bounded with margin here). NaN or
+// infinity fails the test.
+__device__ __forceinline__ bool scatter_small(const Scat& s) {
+  if (s.b[0] < -1000 || s.b[1] < -1000 || s.b[2] < -1000) return false;
+  bool ok = fabsf(s.mass) < 0.9f;   // each comparison is false for NaN
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float r = fabsf(s.mv[i]) + 2.0f * ((fabsf(s.aff[i]) + fabsf(s.aff[3 + i])) + fabsf(s.aff[6 + i]));
+    ok = ok && r < 0.9f;
+  }
+  return ok;
+}
+
 // 27-node scatter of mpm.js:328-349 into the shared tile (planar channels) or the global grid.
-__device__ __forceinline__ void scatter_one(const Scat& s, const int32_t* dims, int* __restrict__ grid,
-                                            int* tile, int tile_cap, int o0, int o1, int o2, int ex, int ey,
-                                            bool use_tile) {
+template <bool SMALL>
+__device__ __forceinline__ void scatter_impl(const Scat& s, const int32_t* dims, int* __restrict__ grid,
+                                             int* tile, int o0, int o1, int o2, int ex, int ey, bool use_tile) {
+  constexpr int tile_cap = kTileNodes;
   float wx[3], wy[3], wz[3];
   bspline(s.f[0], wx); bspline(s.f[1], wy); bspline(s.f[2], wz);
+  const int exy = ex * ey;
+  const int t0 = ((s.b[2] - o2) * ey + (s.b[1] - o1)) * ex + (s.b[0] - o0);
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     float dx = (float)a - s.f[0];
@@ -89,45 +129,104 @@ __device__ __forceinline__ void scatter_one(const Scat& s, const int32_t* dims, 
         float dz = (float)c - s.f[2];
         float wt = wab * wz[c];
         float r0 = s0 + s.aff[6] * dz, r1 = s1 + s.aff[7] * dz, r2 = s2 + s.aff[8] * dz;
-        int32_t q0 = to_fixed(wt * (s.mv[0] + r0));
-        int32_t q1 = to_fixed(wt * (s.mv[1] + r1));
-        int32_t q2 = to_fixed(wt * (s.mv[2] + r2));
-        int32_t q3 = to_fixed(wt * s.mass);
-        int gx = s.b[0] + a, gy = s.b[1] + b, gz = s.b[2] + c;
+        const float m0 = wt * (s.mv[0] + r0), m1 = wt * (s.mv[1] + r1), m2 = wt * (s.mv[2] + r2);
+        const float m3v = wt * s.mass;
+        int32_t q0, q1, q2, q3;
+        if (SMALL) {
+          q0 = to_fixed_small(m0); q1 = to_fixed_small(m1); q2 = to_fixed_small(m2); q3 = to_fixed_small(m3v);
+        } else {
+          q0 = to_fixed(m0); q1 = to_fixed(m1); q2 = to_fixed(m2); q3 = to_fixed(m3v);
+        }
         if (use_tile) {
-          int ti = ((gz - o2) * ey + (gy - o1)) * ex + (gx - o0);
+          const int ti = t0 + a + ex * b + exy * c;
           atomicAdd(&tile[ti], q0);
           atomicAdd(&tile[tile_cap + ti], q1);
           atomicAdd(&tile[2 * tile_cap + ti], q2);
           atomicAdd(&tile[3 * tile_cap + ti], q3);
-        } else if (in_grid(gx, gy, gz, dims)) {
-          size_t gi = 4 * ((size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz));
-          atomicAdd(&grid[gi], q0);
-          atomicAdd(&grid[gi + 1], q1);
-          atomicAdd(&grid[gi + 2], q2);
-          atomicAdd(&grid[gi + 3], q3);
+        } else {
+          const int gx = s.b[0] + a, gy = s.b[1] + b, gz = s.b[2] + c;
+          if (in_grid(gx, gy, gz, dims)) {
+            size_t gi = 4 * ((size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz));
+            atomicAdd(&grid[gi], q0);
+            atomicAdd(&grid[gi + 1], q1);
+            atomicAdd(&grid[gi + 2], q2);
+            atomicAdd(&grid[gi + 3], q3);
+          }
         }
       }
     }
   }
 }
 
-// CTA-wide P2G of up to PPT particles per thread: AABB of the bases (mpm.js:353-377), tile if it
-// fits (mpm.js:379-380), scatter, flush of the non-zero tile nodes with global i32 atomics (mpm.js:385-399).
-template <int PPT>
-__device__ __forceinline__ void cta_scatter(const Scat (&s)[PPT], const bool (&valid)[PPT], const int32_t* dims,
-                                            int* __restrict__ grid, bool force_global, int tile_cap,
-                                            int* tile, int* sbox) {
+__device__ __forceinline__ void scatter_one(const Scat& s, const int32_t* dims, int* __restrict__ grid,
+                                            int* tile, int o0, int o1, int o2, int ex, int ey, bool use_tile) {
+  if (scatter_small(s)) scatter_impl<true>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
+  else scatter_impl<false>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
+}
+
+// P2G inputs of the CTA's particles are staged in shared memory (SoA, kScatWords words per particle)
+// between the per-particle phase and the CTA-wide scatter, so no thread keeps them in registers.
+constexpr int kScatWords = 19;
+
+// A copy of a particle that contributes nothing (mass, momentum and affine zero; the base, which lies
+// inside the chunk's box, stays): lets idle lanes run the scatter on the same path as the others.
+__device__ __forceinline__ void scat_silence(Scat& s) {
+  s.mass = 0.0f;
+  s.mv[0] = s.mv[1] = s.mv[2] = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 9; q++) s.aff[q] = 0.0f;
+}
+
+__device__ __forceinline__ void scat_store(float* sc, int chunk, int slot, const Scat& s) {
+  sc[0 * chunk + slot] = __int_as_float(s.b[0]);
+  sc[1 * chunk + slot] = __int_as_float(s.b[1]);
+  sc[2 * chunk + slot] = __int_as_float(s.b[2]);
+  sc[3 * chunk + slot] = s.f[0];
+  sc[4 * chunk + slot] = s.f[1];
+  sc[5 * chunk + slot] = s.f[2];
+#pragma unroll
+  for (int q = 0; q < 9; q++) sc[(6 + q) * chunk + slot] = s.aff[q];
+  sc[15 * chunk + slot] = s.mv[0];
+  sc[16 * chunk + slot] = s.mv[1];
+  sc[17 * chunk + slot] = s.mv[2];
+  sc[18 * chunk + slot] = s.mass;
+}
+__device__ __forceinline__ void scat_load(const float* sc, int chunk, int slot, Scat& s) {
+  s.b[0] = __float_as_int(sc[0 * chunk + slot]);
+  s.b[1] = __float_as_int(sc[1 * chunk + slot]);
+  s.b[2] = __float_as_int(sc[2 * chunk + slot]);
+  s.f[0] = sc[3 * chunk + slot];
+  s.f[1] = sc[4 * chunk + slot];
+  s.f[2] = sc[5 * chunk + slot];
+#pragma unroll
+  for (int q = 0; q < 9; q++) s.aff[q] = sc[(6 + q) * chunk + slot];
+  s.mv[0] = sc[15 * chunk + slot];
+  s.mv[1] = sc[16 * chunk + slot];
+  s.mv[2] = sc[17 * chunk + slot];
+  s.mass = sc[18 * chunk + slot];
+}
+
+// CTA-wide P2G: AABB of the bases (mpm.js:353-377), tile if it fits (mpm.js:379-380), scatter,
+// flush of the non-zero tile nodes with global i32 atomics (mpm.js:385-399). The particles come from
+// `reg` (one per thread, valid if has_reg) when sc == nullptr, else from the `count` staged copies.
+__device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const float* sc, int chunk, int count,
+                                            const int32_t* dims, int* __restrict__ grid, bool force_global,
+                                            int tile_nodes, int* tile, int* sbox) {
+  constexpr int tile_cap = kTileNodes;
   const int tid = threadIdx.x;
   if (tid < 3) { sbox[tid] = 0x3fffffff; sbox[3 + tid] = -0x3fffffff; }
-  __syncthreads();
+  cta_sync();
   int lo0 = 0x3fffffff, lo1 = 0x3fffffff, lo2 = 0x3fffffff;
   int hi0 = -0x3fffffff, hi1 = -0x3fffffff, hi2 = -0x3fffffff;
-#pragma unroll
-  for (int k = 0; k < PPT; k++) {
-    if (valid[k]) {
-      lo0 = min(lo0, s[k].b[0]); lo1 = min(lo1, s[k].b[1]); lo2 = min(lo2, s[k].b[2]);
-      hi0 = max(hi0, s[k].b[0]); hi1 = max(hi1, s[k].b[1]); hi2 = max(hi2, s[k].b[2]);
+  if (sc == nullptr) {
+    if (has_reg) {
+      lo0 = hi0 = reg.b[0]; lo1 = hi1 = reg.b[1]; lo2 = hi2 = reg.b[2];
+    }
+  } else {
+    for (int slot = tid; slot < count; slot += blockDim.x) {   // count is a multiple of the CTA size here
+      const int b0 = __float_as_int(sc[slot]), b1 = __float_as_int(sc[chunk + slot]), b2 = __float_as_int(sc[2 * chunk + slot]);
+      lo0 = min(lo0, b0); lo1 = min(lo1, b1); lo2 = min(lo2, b2);
+      hi0 = max(hi0, b0); hi1 = max(hi1, b1); hi2 = max(hi2, b2);
     }
   }
   lo0 = __reduce_min_sync(0xffffffffu, lo0); lo1 = __reduce_min_sync(0xffffffffu, lo1);
@@ -138,25 +237,32 @@ __device__ __forceinline__ void cta_scatter(const Scat (&s)[PPT], const bool (&v
     atomicMin(&sbox[0], lo0); atomicMin(&sbox[1], lo1); atomicMin(&sbox[2], lo2);
     atomicMax(&sbox[3], hi0); atomicMax(&sbox[4], hi1); atomicMax(&sbox[5], hi2);
   }
-  __syncthreads();
+  cta_sync();
   const int o0 = sbox[0], o1 = sbox[1], o2 = sbox[2];
   const int ex = sbox[3] - o0 + 3, ey = sbox[4] - o1 + 3, ez = sbox[5] - o2 + 3;
-  __syncthreads();   // sbox is reused by the next chunk
+  cta_sync();   // sbox is reused by the next chunk
   if (ex <= 0 || ey <= 0 || ez <= 0) return;    // no valid particle in the chunk
   const long long tn = (long long)ex * ey * ez;
-  const bool use_tile = tn <= tile_cap && !force_global;
+  const bool use_tile = tn <= tile_nodes && !force_global;
   const int tnodes = (int)(use_tile ? tn : 0);
   if (use_tile) {
     for (int t = tid; t < tnodes; t += blockDim.x) {
       tile[t] = 0; tile[tile_cap + t] = 0; tile[2 * tile_cap + t] = 0; tile[3 * tile_cap + t] = 0;
     }
-    __syncthreads();
+    cta_sync();
   }
-#pragma unroll
-  for (int k = 0; k < PPT; k++)
-    if (valid[k]) scatter_one(s[k], dims, grid, tile, tile_cap, o0, o1, o2, ex, ey, use_tile);
+  if (sc == nullptr) {
+    if (has_reg) scatter_one(reg, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
+  } else {
+#pragma unroll 1
+    for (int slot = tid; slot < count; slot += blockDim.x) {
+      Scat s;
+      scat_load(sc, chunk, slot, s);
+      scatter_one(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
+    }
+  }
   if (use_tile) {
-    __syncthreads();
+    cta_sync();
     for (int t = tid; t < tnodes; t += blockDim.x) {
       int m = tile[3 * tile_cap + t], mx = tile[t], my = tile[tile_cap + t], mz = tile[2 * tile_cap + t];
       if ((m | mx | my | mz) != 0) {
@@ -171,40 +277,42 @@ __device__ __forceinline__ void cta_scatter(const Scat (&s)[PPT], const bool (&v
         }
       }
     }
-    __syncthreads();   // the tile is reused by the next chunk
   }
+  cta_sync();   // the tile and the staged inputs are reused by the next chunk
 }
 
 // ------------------------------------------------------------------ P2G kernel (mpm.js:306-401)
 template <int PPT>
-__global__ void __launch_bounds__(kCtaThreads) k_p2g(TickInfo t) {
-  extern __shared__ int smem[];
+__global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t) {
+  extern __shared__ __align__(16) int smem[];
   int* tile = smem;
-  int* sbox = smem + 4 * t.tile_nodes;
-  for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
-    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, chunk)];
+  int* sbox = smem + 4 * kTileNodes;
+  float* sc = reinterpret_cast<float*>(sbox + 8);
+  constexpr int chunk = kCtaThreads * PPT;
+  for (uint32_t c = blockIdx.x; c < t.pchunks; c += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, c)];
     const uint32_t flags = ts.flags;
     if (!(flags & F_P2G)) continue;
     const SceneParams* prm = ts.prm;
-    const int first = (int)(chunk - ts.pchunk_begin) * (kCtaThreads * PPT);
+    const int first = (int)(c - ts.pchunk_begin) * chunk;
+    const int count = min(chunk, ts.n - first);
     const int32_t dims[3] = {prm->dims[0], prm->dims[1], prm->dims[2]};
     const float4* src = ts.P;
     const int64_t cap = ts.cap;
-    Scat s[PPT];
-    bool valid[PPT];
+    Scat reg;
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-      const int i = first + k * kCtaThreads + threadIdx.x;
-      valid[k] = i < ts.n;
-      if (valid[k]) {
-        float4 x = __ldg(&src[i]), v = __ldg(&src[cap + i]);
-        float4 c0 = __ldg(&src[2 * cap + i]), c1 = __ldg(&src[3 * cap + i]), c2 = __ldg(&src[4 * cap + i]);
-        float t01 = __ldg(&src[5 * cap + i].w), t02 = __ldg(&src[6 * cap + i].w), t12 = __ldg(&src[7 * cap + i].w);
-        prep_scatter(s[k], x, v, c0, c1, c2, t01, t02, t12, prm);
-      }
+      const bool valid = k * kCtaThreads + (int)threadIdx.x < count;
+      const int64_t i = first + min(k * kCtaThreads + (int)threadIdx.x, count - 1);
+      float4 x = __ldg(&src[i]), v = __ldg(&src[cap + i]);
+      float4 c0 = __ldg(&src[2 * cap + i]), c1 = __ldg(&src[3 * cap + i]), c2 = __ldg(&src[4 * cap + i]);
+      float t01 = __ldg(&src[5 * cap + i].w), t02 = __ldg(&src[6 * cap + i].w), t12 = __ldg(&src[7 * cap + i].w);
+      prep_scatter(reg, x, v, c0, c1, c2, t01, t02, t12, prm);
+      if (!valid) scat_silence(reg);
+      if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + threadIdx.x, reg);
     }
-    cta_scatter<PPT>(s, valid, dims, reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0,
-                     t.tile_nodes, tile, sbox);
+    cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
+                reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox);
   }
 }
 
@@ -316,9 +424,14 @@ __global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
 }
 
 // ------------------------------------------------------------------ G2P (mpm.js:474-560)
+// The 27-node gather reads the CTA's shared tile (TILE: node (a,b,c) of the stencil at
+// t0 + a + sx*b + sxy*c, always inside) or, when the CTA's stencils did not fit the tile, the
+// global grid with bounds checks (nodes outside the grid read as zero).
+template <bool TILE>
 __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, float4& C1, float4& C2,
                                              float4& F0, float4& F1, float4& F2, const SceneParams* prm,
-                                             const float4* __restrict__ grid) {
+                                             const float4* __restrict__ grid, const float4* tilef, int o0,
+                                             int o1, int o2, int sx, int sxy) {
   const int32_t dx0 = prm->dims[0], dx1 = prm->dims[1], dx2 = prm->dims[2];
   const int b0 = base_of(X.x, dx0), b1 = base_of(X.y, dx1), b2 = base_of(X.z, dx2);
   const float f0 = X.x - (float)b0, f1 = X.y - (float)b1, f2 = X.z - (float)b2;
@@ -327,7 +440,8 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
   v3 v = V(0.0f, 0.0f, 0.0f);
   m3 B;
   B.c[0] = V(0.0f, 0.0f, 0.0f); B.c[1] = V(0.0f, 0.0f, 0.0f); B.c[2] = V(0.0f, 0.0f, 0.0f);
-#pragma unroll
+  const int t0 = TILE ? ((b2 - o2) * (sxy / sx) + (b1 - o1)) * sx + (b0 - o0) : 0;
+#pragma unroll 1
   for (int a = 0; a < 3; a++) {
     const float dpx = (float)a - f0;
 #pragma unroll
@@ -338,17 +452,24 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
       for (int c = 0; c < 3; c++) {
         const float dpz = (float)c - f2;
         const float wt = wab * wz[c];
-        const int gx = b0 + a, gy = b1 + b, gz = b2 + c;
-        v3 gv = V(0.0f, 0.0f, 0.0f);
-        if ((unsigned)gx < (unsigned)dx0 && (unsigned)gy < (unsigned)dx1 && (unsigned)gz < (unsigned)dx2) {
-          const float4 n = __ldg(&grid[(size_t)gx + (size_t)dx0 * ((size_t)gy + (size_t)dx1 * (size_t)gz)]);
+        v3 gv;
+        if (TILE) {
+          const float4 n = tilef[t0 + a + sx * b + sxy * c];
           gv = V(n.x, n.y, n.z);
+        } else {
+          const int gx = b0 + a, gy = b1 + b, gz = b2 + c;
+          gv = V(0.0f, 0.0f, 0.0f);
+          if ((unsigned)gx < (unsigned)dx0 && (unsigned)gy < (unsigned)dx1 && (unsigned)gz < (unsigned)dx2) {
+            const float4 n = __ldg(&grid[(size_t)gx + (size_t)dx0 * ((size_t)gy + (size_t)dx1 * (size_t)gz)]);
+            gv = V(n.x, n.y, n.z);
+          }
         }
         const v3 t = vscale(wt, gv);
         v = vadd(v, t);
-        B.c[0] = vadd(B.c[0], vscale(dpx, t));
-        B.c[1] = vadd(B.c[1], vscale(dpy, t));
-        B.c[2] = vadd(B.c[2], vscale(dpz, t));
+        // B += outer3(t, dpos) with one fused multiply-add per entry (the oracle uses fmaf alike)
+        B.c[0] = V(__fmaf_rn(dpx, t.x, B.c[0].x), __fmaf_rn(dpx, t.y, B.c[0].y), __fmaf_rn(dpx, t.z, B.c[0].z));
+        B.c[1] = V(__fmaf_rn(dpy, t.x, B.c[1].x), __fmaf_rn(dpy, t.y, B.c[1].y), __fmaf_rn(dpy, t.z, B.c[1].z));
+        B.c[2] = V(__fmaf_rn(dpz, t.x, B.c[2].x), __fmaf_rn(dpz, t.y, B.c[2].y), __fmaf_rn(dpz, t.z, B.c[2].z));
       }
     }
   }
@@ -460,43 +581,115 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
   F2 = make_float4(F.c[2].x, F.c[2].y, F.c[2].z, t12);
 }
 
+// AABB of the bases of the chunk's particles (x of each slot given by xs), into sbox[0..5].
 template <int PPT>
-__global__ void __launch_bounds__(kCtaThreads) k_g2p(TickInfo t, const uint32_t* __restrict__ perm) {
-  extern __shared__ int smem[];
+__device__ __forceinline__ void cta_base_box(const float4 (&xs)[PPT], int count, const int32_t* dims, int* sbox) {
+  const int tid = threadIdx.x;
+  int lo0 = 0x3fffffff, lo1 = 0x3fffffff, lo2 = 0x3fffffff;
+  int hi0 = -0x3fffffff, hi1 = -0x3fffffff, hi2 = -0x3fffffff;
+  (void)count;   // lanes past the end hold a copy of the last particle: inside the box already
+#pragma unroll
+  for (int k = 0; k < PPT; k++) {
+    const int b0 = base_of(xs[k].x, dims[0]), b1 = base_of(xs[k].y, dims[1]), b2 = base_of(xs[k].z, dims[2]);
+    lo0 = min(lo0, b0); lo1 = min(lo1, b1); lo2 = min(lo2, b2);
+    hi0 = max(hi0, b0); hi1 = max(hi1, b1); hi2 = max(hi2, b2);
+  }
+  if (tid < 3) { sbox[tid] = 0x3fffffff; sbox[3 + tid] = -0x3fffffff; }
+  cta_sync();
+  lo0 = __reduce_min_sync(0xffffffffu, lo0); lo1 = __reduce_min_sync(0xffffffffu, lo1);
+  lo2 = __reduce_min_sync(0xffffffffu, lo2);
+  hi0 = __reduce_max_sync(0xffffffffu, hi0); hi1 = __reduce_max_sync(0xffffffffu, hi1);
+  hi2 = __reduce_max_sync(0xffffffffu, hi2);
+  if ((tid & 31) == 0) {
+    atomicMin(&sbox[0], lo0); atomicMin(&sbox[1], lo1); atomicMin(&sbox[2], lo2);
+    atomicMax(&sbox[3], hi0); atomicMax(&sbox[4], hi1); atomicMax(&sbox[5], hi2);
+  }
+  cta_sync();
+}
+
+// G2P of a chunk: gather tile (the grid nodes under the chunk's stencils, staged once in shared
+// memory), per-particle G2P, store, then the fused P2G of the next substep through the same tile.
+template <int PPT>
+__global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t, const uint32_t* __restrict__ perm) {
+  extern __shared__ __align__(16) int smem[];
   int* tile = smem;
-  int* sbox = smem + 4 * t.tile_nodes;
-  for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
-    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, chunk)];
+  float4* tilef = reinterpret_cast<float4*>(smem);
+  int* sbox = smem + 4 * kTileNodes;
+  float* sc = reinterpret_cast<float*>(sbox + 8);
+  constexpr int chunk = kCtaThreads * PPT;
+  const int tid = threadIdx.x;
+  for (uint32_t c = blockIdx.x; c < t.pchunks; c += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, c)];
     const uint32_t flags = ts.flags;
     const SceneParams* prm = ts.prm;
-    const int first = (int)(chunk - ts.pchunk_begin) * (kCtaThreads * PPT);
+    const int first = (int)(c - ts.pchunk_begin) * chunk;
+    const int count = min(chunk, ts.n - first);
     const bool fuse = (flags & F_FUSE) != 0;
     const bool gather = (flags & F_GATHER) != 0;
     const float4* Pin = ts.P;
     float4* P = gather ? ts.Palt : ts.P;
     const int64_t cap = ts.cap;
     const float4* grid = reinterpret_cast<const float4*>(ts.grid);
-    Scat s[PPT];
-    bool valid[PPT];
+    const int32_t dims[3] = {prm->dims[0], prm->dims[1], prm->dims[2]};
+    // 1. positions and the box of the old stencils. Lanes past the end of a partial chunk work on a
+    // copy of the chunk's last particle and store nothing: every lane of a warp takes the same path
+    // up to each CTA barrier (a barrier completes for a warp once some of its lanes arrive, so lanes
+    // must not reach it ahead of their warp-mates).
+    float4 xs[PPT];
+    int64_t js[PPT];
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-      const int i = first + k * kCtaThreads + threadIdx.x;
-      valid[k] = i < ts.n;
-      if (valid[k]) {
-        const int64_t j = gather ? (int64_t)__ldg(&perm[ts.seg_base + i]) : (int64_t)i;
-        float4 x = Pin[j], v = Pin[cap + j], c0 = Pin[2 * cap + j], c1 = Pin[3 * cap + j], c2 = Pin[4 * cap + j];
-        float4 f0 = Pin[5 * cap + j], f1 = Pin[6 * cap + j], f2 = Pin[7 * cap + j];
-        g2p_particle(x, v, c0, c1, c2, f0, f1, f2, prm, grid);
-        P[i] = x; P[cap + i] = v; P[2 * cap + i] = c0; P[3 * cap + i] = c1; P[4 * cap + i] = c2;
-        P[5 * cap + i] = f0; P[6 * cap + i] = f1; P[7 * cap + i] = f2;
-        if (flags & F_KEYS) ts.keys[i] = block_key(x.x, x.y, x.z, prm->num_blocks);
-        if (fuse) prep_scatter(s[k], x, v, c0, c1, c2, f0.w, f1.w, f2.w, prm);
+      const int slot = min(k * kCtaThreads + tid, count - 1);
+      js[k] = gather ? (int64_t)__ldg(&perm[ts.seg_base + first + slot]) : (int64_t)(first + slot);
+      xs[k] = __ldcs(&Pin[js[k]]);
+    }
+    cta_base_box<PPT>(xs, count, dims, sbox);
+    const int o0 = sbox[0], o1 = sbox[1], o2 = sbox[2];
+    const int ex = sbox[3] - o0 + 3, ey = sbox[4] - o1 + 3, ez = sbox[5] - o2 + 3;
+    const long long gtn = (long long)ex * ey * ez;
+    const bool gtile = ex > 0 && gtn <= t.tile_nodes;
+    // 2. stage the gather tile: vec4f(v, m) of every node under the stencils (zero outside the grid)
+    if (gtile) {
+      for (int q = tid; q < (int)gtn; q += kCtaThreads) {
+        const int lx = q % ex, ly = (q / ex) % ey, lz = q / (ex * ey);
+        const int gx = o0 + lx, gy = o1 + ly, gz = o2 + lz;
+        float4 n = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if ((unsigned)gx < (unsigned)dims[0] && (unsigned)gy < (unsigned)dims[1] && (unsigned)gz < (unsigned)dims[2])
+          n = __ldg(&grid[(size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz)]);
+        tilef[q] = n;
       }
     }
-    if (fuse) {
-      const int32_t dims[3] = {prm->dims[0], prm->dims[1], prm->dims[2]};
-      cta_scatter<PPT>(s, valid, dims, reinterpret_cast<int*>(ts.grid_next), false, t.tile_nodes, tile, sbox);
+    cta_sync();
+    // 3. per-particle G2P
+    Scat reg;
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+      const bool valid = k * kCtaThreads + tid < count;
+      const int slot = min(k * kCtaThreads + tid, count - 1);
+      const int64_t i = first + slot, j = js[k];
+      float4 x = xs[k], v = __ldcs(&Pin[cap + j]), c0 = __ldcs(&Pin[2 * cap + j]), c1 = __ldcs(&Pin[3 * cap + j]);
+      float4 c2 = __ldcs(&Pin[4 * cap + j]), f0 = __ldcs(&Pin[5 * cap + j]), f1 = __ldcs(&Pin[6 * cap + j]);
+      float4 f2 = __ldcs(&Pin[7 * cap + j]);
+      if (gtile) g2p_particle<true>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, o0, o1, o2, ex, ex * ey);
+      else g2p_particle<false>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, 0, 0, 0, 1, 1);
+      if (valid) {
+        __stcs(&P[i], x); __stcs(&P[cap + i], v); __stcs(&P[2 * cap + i], c0); __stcs(&P[3 * cap + i], c1);
+        __stcs(&P[4 * cap + i], c2); __stcs(&P[5 * cap + i], f0); __stcs(&P[6 * cap + i], f1);
+        __stcs(&P[7 * cap + i], f2);
+        if (flags & F_KEYS) ts.keys[i] = block_key(x.x, x.y, x.z, prm->num_blocks);
+      }
+      if (fuse) {
+        prep_scatter(reg, x, v, c0, c1, c2, f0.w, f1.w, f2.w, prm);
+        if (!valid) scat_silence(reg);
+        if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + tid, reg);
+      }
     }
+    // 4. P2G of the next substep through the same shared memory (cta_scatter synchronises first)
+    if (fuse)
+      cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
+                  reinterpret_cast<int*>(ts.grid_next), false, t.tile_nodes, tile, sbox);
+    else
+      cta_sync();
   }
 }
 
@@ -552,11 +745,15 @@ __global__ void k_positions(const float4* __restrict__ P, int64_t off, int64_t n
 }
 
 // ------------------------------------------------------------------ launchers
-int p2g_smem_bytes(int tile_nodes) { return tile_nodes * 16 + 32; }
+int p2g_smem_bytes(int tile_nodes, int ppt) {
+  (void)tile_nodes;
+  return kTileNodes * 16 + 32 + (ppt > 1 ? kScatWords * 4 * kCtaThreads * ppt : 0);
+}
+int max_tile_nodes() { return kTileNodes; }
 
 template <int PPT>
 static void set_smem_attr(int tile_nodes) {
-  int bytes = p2g_smem_bytes(tile_nodes);
+  int bytes = p2g_smem_bytes(tile_nodes, PPT);
   if (bytes > 48 * 1024) {
     cudaFuncSetAttribute(k_p2g<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_g2p<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -566,7 +763,7 @@ static void set_smem_attr(int tile_nodes) {
 void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st) {
   if (t.pchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
-  int smem = p2g_smem_bytes(t.tile_nodes);
+  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kCtaThreads);
   switch (t.chunk / kCtaThreads) {
     case 1: k_p2g<1><<<ctas, kCtaThreads, smem, st>>>(t); break;
     case 4: k_p2g<4><<<ctas, kCtaThreads, smem, st>>>(t); break;
@@ -576,7 +773,7 @@ void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st) {
 void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st) {
   if (t.pchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
-  int smem = p2g_smem_bytes(t.tile_nodes);
+  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kCtaThreads);
   switch (t.chunk / kCtaThreads) {
     case 1: k_g2p<1><<<ctas, kCtaThreads, smem, st>>>(t, perm); break;
     case 4: k_g2p<4><<<ctas, kCtaThreads, smem, st>>>(t, perm); break;
@@ -632,11 +829,15 @@ void configure_kernels(int tile_nodes) {
   set_smem_attr<4>(tile_nodes);
 }
 
-int occupancy_ctas(int which, int tile_nodes) {
+int occupancy_ctas(int which, int tile_nodes, int ppt) {
   int n = 0;
-  int smem = p2g_smem_bytes(tile_nodes);
+  int smem = p2g_smem_bytes(tile_nodes, ppt);
   switch (which) {
-    case 0: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<2>, kCtaThreads, smem); break;
+    case 0:
+      if (ppt == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<1>, kCtaThreads, smem);
+      else if (ppt == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<4>, kCtaThreads, smem);
+      else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<2>, kCtaThreads, smem);
+      break;
     case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<2>, kCtaThreads, smem); break;
     case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_grid, kCtaThreads, 0); break;
     case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<1>, kCtaThreads, smem); break;

@@ -105,15 +105,15 @@ static int world_init(si_world* w) {
 
 int world_configure(si_world* w, int ppt, int tile_nodes) {
   if (ppt != 1 && ppt != 2 && ppt != 4) return si_fail(SI_EINVAL, "particles per CTA must be 256, 512 or 1024");
-  if (tile_nodes < 343 || p2g_smem_bytes(tile_nodes) > w->max_smem_optin)
+  if (tile_nodes < 343 || tile_nodes > max_tile_nodes() || p2g_smem_bytes(tile_nodes, ppt) > w->max_smem_optin)
     return si_fail(SI_EINVAL, "tile capacity must hold at least 7^3 nodes and fit shared memory");
   w->ppt = ppt;
   w->tile_nodes = tile_nodes;
   configure_kernels(tile_nodes);
   const int which_g2p = ppt == 1 ? 3 : (ppt == 4 ? 4 : 1);
-  w->ctas_p2g = w->sms * occupancy_ctas(0, tile_nodes);
-  w->ctas_g2p = w->sms * occupancy_ctas(which_g2p, tile_nodes);
-  w->ctas_grid = w->sms * occupancy_ctas(2, tile_nodes);
+  w->ctas_p2g = w->sms * occupancy_ctas(0, tile_nodes, ppt);
+  w->ctas_g2p = w->sms * occupancy_ctas(which_g2p, tile_nodes, ppt);
+  w->ctas_grid = w->sms * occupancy_ctas(2, tile_nodes, ppt);
   w->ctas_misc = w->sms * 4;
   cudaGetLastError();
   w->graphs.clear();

