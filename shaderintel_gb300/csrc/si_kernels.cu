@@ -107,22 +107,40 @@ __device__ __forceinline__ bool scatter_small(const Scat& s) {
 }
 
 // 27-node scatter of mpm.js:328-349 into the shared tile (planar channels) or the global grid.
+// Lanes whose particles share a base node would hit the same 27 addresses step for step and their
+// atomics would serialise; so each lane visits the x offsets rotated by (lane mod 3) and the y
+// offsets by (lane / 3 mod 3). Every node's contribution is computed by the same expression as in
+// the unrotated order, so the i32 sums are unchanged.
 template <bool SMALL>
 __device__ __forceinline__ void scatter_impl(const Scat& s, const int32_t* dims, int* __restrict__ grid,
                                              int* tile, int o0, int o1, int o2, int ex, int ey, bool use_tile) {
   constexpr int tile_cap = kTileNodes;
   float wx[3], wy[3], wz[3];
   bspline(s.f[0], wx); bspline(s.f[1], wy); bspline(s.f[2], wz);
+  const int lane = threadIdx.x & 31;
+  const int ra = lane % 3, rb = (lane / 3) % 3;
+  int ia[3], ib[3];
+  float wa[3], wb[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int a = k + ra >= 3 ? k + ra - 3 : k + ra;
+    const int b = k + rb >= 3 ? k + rb - 3 : k + rb;
+    ia[k] = a; ib[k] = b;
+    wa[k] = a == 0 ? wx[0] : (a == 1 ? wx[1] : wx[2]);
+    wb[k] = b == 0 ? wy[0] : (b == 1 ? wy[1] : wy[2]);
+  }
   const int exy = ex * ey;
   const int t0 = ((s.b[2] - o2) * ey + (s.b[1] - o1)) * ex + (s.b[0] - o0);
 #pragma unroll
-  for (int a = 0; a < 3; a++) {
+  for (int ka = 0; ka < 3; ka++) {
+    const int a = ia[ka];
     float dx = (float)a - s.f[0];
     float ax0 = s.aff[0] * dx, ax1 = s.aff[1] * dx, ax2 = s.aff[2] * dx;
 #pragma unroll
-    for (int b = 0; b < 3; b++) {
+    for (int kb = 0; kb < 3; kb++) {
+      const int b = ib[kb];
       float dy = (float)b - s.f[1];
-      float wab = wx[a] * wy[b];
+      float wab = wa[ka] * wb[kb];
       float s0 = ax0 + s.aff[3] * dy, s1 = ax1 + s.aff[4] * dy, s2 = ax2 + s.aff[5] * dy;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
@@ -158,14 +176,16 @@ __device__ __forceinline__ void scatter_impl(const Scat& s, const int32_t* dims,
   }
 }
 
+// Every lane of the warp calls this (idle lanes with a silenced copy); the fast conversion is chosen
+// per warp so the lanes stay on one path.
 __device__ __forceinline__ void scatter_one(const Scat& s, const int32_t* dims, int* __restrict__ grid,
                                             int* tile, int o0, int o1, int o2, int ex, int ey, bool use_tile) {
-  if (scatter_small(s)) scatter_impl<true>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
+  if (__all_sync(0xffffffffu, scatter_small(s))) scatter_impl<true>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
   else scatter_impl<false>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
 }
 
-// P2G inputs of the CTA's particles are staged in shared memory (SoA, kScatWords words per particle)
-// between the per-particle phase and the CTA-wide scatter, so no thread keeps them in registers.
+// P2G inputs of the CTA's particles, staged in shared memory (SoA, kScatWords words per particle)
+// when a thread handles more than one particle of a chunk.
 constexpr int kScatWords = 19;
 
 // A copy of a particle that contributes nothing (mass, momentum and affine zero; the base, which lies
@@ -252,7 +272,7 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
     cta_sync();
   }
   if (sc == nullptr) {
-    if (has_reg) scatter_one(reg, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
+    scatter_one(reg, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);   // every lane (has_reg is true)
   } else {
 #pragma unroll 1
     for (int slot = tid; slot < count; slot += blockDim.x) {

@@ -300,6 +300,14 @@ class MPM:
         check(L.lib().si_mpm_add_particles(self._h, fptr(rec), n, ctypes.byref(added)))
         return added.value
 
+    def addRecords(self, records):
+        """Append raw particle records (32 floats each, the reference layout) up to the capacity;
+        returns how many were taken (the upload half of add(), mpm.js:228-230)."""
+        rec = np.ascontiguousarray(records, np.float32).reshape(-1, 32)
+        added = ctypes.c_int64()
+        check(L.lib().si_mpm_add_particles(self._h, fptr(rec), len(rec), ctypes.byref(added)))
+        return added.value
+
     def clear(self):
         """Remove every particle and forget the materials (mpm.js:238-242)."""
         check(L.lib().si_mpm_clear(self._h))

@@ -233,11 +233,7 @@ def test_trajectory_interleaved_materials_bit_exact():
     sim.clear()
     for name in ("water", "jelly", "snow", "sand"):
         sim._material(name)
-    sim.writeParticles_raw = None
-    from shaderintel_gb300 import _lib as L
-    added = __import__("ctypes").c_int64()
-    L.check(L.lib().si_mpm_add_particles(sim._h, L.fptr(np.ascontiguousarray(rec)), n, __import__("ctypes").byref(added)))
-    assert added.value == n
+    assert sim.addRecords(rec) == n
     mats, cols, ncol, grav, vol4 = tables(sim)
     rec0 = sim.readParticles()
     sim.step(K=24)
