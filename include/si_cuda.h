@@ -146,6 +146,22 @@ int si_mpm_read_grid(si_mpm* h, int32_t* nodes4);
 int si_mpm_read_bins(si_mpm* h, uint32_t* keys, uint32_t* starts);
 int si_mpm_sync(si_mpm* h);
 
+/* Allocation-free block binning (no counterpart in the reference: its sort always runs on buffers
+ * the MPM object allocated). For callers that must not allocate device memory themselves or through
+ * this library: a host whose allocator owns all of the GPU's memory, a stream being recorded into a
+ * CUDA graph, a frame loop that cannot take the device-wide synchronisation of cudaFree. Given n
+ * positions on the device (x at x[i * stride_floats + 0..2]) and the grid dims, it writes, all on
+ * the device: keys[n] (the block key of each particle, mpm.js:567-569), perm[n] (the stable sorted
+ * order: entry d is the index of the particle that goes to slot d) and starts[numBlocks + 1] (the
+ * exclusive scan of the block counts). Work is queued on `stream` (NULL: the default stream).
+ * Its scratch is one fixed device array inside this library (about 4.3 MB per GPU that loads it,
+ * kept until the process exits): n may be at most 262144, larger n fails with SI_EINVAL. Every
+ * call uses the same array, so calls that overlap on the GPU (other streams, other threads) race:
+ * order them. The first call on each device looks up the array's address; make that first call
+ * before any stream capture. No part of the scratch needs to start at zero. */
+int si_block_sort_noalloc(const float* x, int64_t stride_floats, int32_t n, const int32_t dims[3],
+                          uint32_t* keys, uint32_t* perm, uint32_t* starts, void* stream);
+
 /* ---------------------------------------------------------------- host helpers (no device)
  * The reference's host-side arithmetic, in f64 as JavaScript does it, so that every host that
  * drives this library builds bit-identical scenes. */

@@ -84,6 +84,8 @@ SIGNATURES = {
     "si_mpm_read_grid": (ctypes.c_int, [vp, c_int32_p]),
     "si_mpm_read_bins": (ctypes.c_int, [vp, c_uint32_p, c_uint32_p]),
     "si_mpm_sync": (ctypes.c_int, [vp]),
+    "si_block_sort_noalloc": (ctypes.c_int, [c_float_p, ctypes.c_int64, ctypes.c_int32, c_int32_p, c_uint32_p,
+                                             c_uint32_p, c_uint32_p, vp]),
     "si_material_preset": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(si_material_def)]),
     "si_material_row": (ctypes.c_int, [ctypes.POINTER(si_material_def), ctypes.c_int32, c_float_p]),
     "si_sample_shape": (ctypes.c_int, [ctypes.c_int32, c_double_p, c_double_p, ctypes.c_double, ctypes.c_double,

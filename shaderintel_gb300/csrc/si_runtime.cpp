@@ -39,6 +39,8 @@ int si_fail(int code, const std::string& msg) {
   return code;
 }
 
+extern "C" int si_fail_c(int code, const char* msg) { return si_fail(code, msg ? msg : ""); }
+
 #define CK(call)                                                                               \
   do {                                                                                         \
     cudaError_t e_ = (call);                                                                   \

@@ -7,7 +7,9 @@
 // waits between CTAs, and yields the reference's counts and starts exactly; each scene's particles
 // stay inside its own segment because the bin ranges are ordered like the segments.
 #include <algorithm>
+#include <mutex>
 
+#include "si_cuda.h"
 #include "si_device.h"
 
 namespace si {
@@ -204,3 +206,123 @@ void launch_scene_starts_all(const TickInfo& t, const uint32_t* sorted_keys, uin
 }
 
 }  // namespace si
+
+// ------------------------------------------------------------------ allocation-free block sort
+// The block binning of _sort() (keys, stable order, starts) for positions the caller already holds
+// on the device, with every intermediate buffer in one file-scope device array instead of memory
+// from cudaMalloc. For callers that must not allocate device memory: a host that has handed the
+// GPU's memory to its own pool, a stream that is being recorded into a CUDA graph, or a frame loop
+// that cannot afford the device-wide synchronisation cudaFree implies.
+namespace si {
+
+constexpr int64_t kNoAllocMaxParticles = 262144;   // the reference MPM's default capacity
+constexpr int64_t kNoAllocTiles = (kNoAllocMaxParticles + kSortTile - 1) / kSortTile;
+// two (key, index) ping-pong pairs, the per-tile digit histogram and the digit totals
+constexpr int64_t kNoAllocWords = 4 * kNoAllocMaxParticles + 256 * kNoAllocTiles + 256;
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
+
+__global__ void k_na_keys(const float* __restrict__ x, int64_t stride, int32_t n, uint32_t num_blocks,
+                          uint32_t* keys_out, uint32_t* skeys, uint32_t* svals) {
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float* p = x + (int64_t)i * stride;
+    const float fx = fminf(fmaxf(p[0], 0.0f), 16777216.0f), fy = fminf(fmaxf(p[1], 0.0f), 16777216.0f);
+    const float fz = fminf(fmaxf(p[2], 0.0f), 16777216.0f);
+    const uint32_t bx = ((uint32_t)fx) / 4u, by = ((uint32_t)fy) / 4u, bz = ((uint32_t)fz) / 4u;
+    auto part = [](uint32_t v) {
+      v &= 0x3ffu;
+      v = (v | (v << 16)) & 0x030000ffu;
+      v = (v | (v << 8)) & 0x0300f00fu;
+      v = (v | (v << 4)) & 0x030c30c3u;
+      v = (v | (v << 2)) & 0x09249249u;
+      return v;
+    };
+    uint32_t k = part(bx) | (part(by) << 1) | (part(bz) << 2);
+    k = k < num_blocks ? k : num_blocks - 1u;
+    keys_out[i] = k;
+    skeys[i] = k;
+    svals[i] = (uint32_t)i;
+  }
+}
+
+__global__ void k_na_starts(const uint32_t* __restrict__ skeys, int32_t n, uint32_t num_blocks, uint32_t* starts) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= num_blocks; k += gridDim.x * blockDim.x) {
+    uint32_t lo = 0, hi = (uint32_t)n;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(&skeys[mid]) < k) lo = mid + 1; else hi = mid;
+    }
+    starts[k] = lo;
+  }
+}
+
+}  // namespace si
+
+extern "C" int si_fail_c(int code, const char* msg);
+
+extern "C" int si_block_sort_noalloc(const float* x, int64_t stride_floats, int32_t n, const int32_t dims[3],
+                                     uint32_t* keys, uint32_t* perm, uint32_t* starts, void* stream) {
+  using namespace si;
+  if (n < 0 || (n > 0 && (!x || !keys || !perm)) || !dims || !starts || stride_floats < 3)
+    return si_fail_c(SI_EINVAL, "si_block_sort_noalloc: bad argument (null pointer, n < 0 or stride < 3)");
+  if (n > kNoAllocMaxParticles)
+    return si_fail_c(SI_EINVAL, "si_block_sort_noalloc: n exceeds the fixed scratch capacity of 262144 particles");
+  int32_t bmax = 0;
+  for (int a = 0; a < 3; a++) {
+    if (dims[a] <= 0 || dims[a] > 4096) return si_fail_c(SI_EINVAL, "si_block_sort_noalloc: dims must be in [1, 4096]");
+    bmax = std::max(bmax, (dims[a] + 3) / 4);
+  }
+  uint32_t bpow = 1;
+  while ((int32_t)bpow < bmax) bpow <<= 1;
+  const uint32_t nb = bpow * bpow * bpow;   // numBlocks of mpm.js:119-121
+  // set-up, once per device and with that device current: the array's device address
+  static std::mutex mu;
+  static uint32_t* base[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return si_fail_c(SI_EDEVICE, "si_block_sort_noalloc: no current CUDA device");
+  uint32_t* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (!base[dev]) {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return si_fail_c(SI_EDEVICE, "si_block_sort_noalloc: cudaGetSymbolAddress of the scratch array failed");
+      }
+      base[dev] = static_cast<uint32_t*>(p);
+    }
+    scratch = base[dev];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int ctas = 1024;
+  if (n == 0) {
+    k_na_starts<<<(unsigned)std::min<uint64_t>((nb + 256) / 256, 4096), 256, 0, st>>>(scratch, 0, nb, starts);
+    return cudaGetLastError() == cudaSuccess ? SI_OK : si_fail_c(SI_EDEVICE, "si_block_sort_noalloc: launch failed");
+  }
+  uint32_t* ka = scratch;
+  uint32_t* va = scratch + kNoAllocMaxParticles;
+  uint32_t* kb = scratch + 2 * kNoAllocMaxParticles;
+  uint32_t* vb = scratch + 3 * kNoAllocMaxParticles;
+  uint32_t* hist = scratch + 4 * kNoAllocMaxParticles;
+  uint32_t* digit_total = hist + 256 * kNoAllocTiles;
+  k_na_keys<<<(unsigned)std::min<int64_t>((n + 255) / 256, ctas), 256, 0, st>>>(x, stride_floats, n, nb, keys, ka, va);
+  int bits = 1;
+  while (bits < 32 && (1ull << bits) < (uint64_t)std::max<uint32_t>(nb, 2u)) bits++;
+  const int passes = (bits + kRadixBits - 1) / kRadixBits;
+  const uint32_t tiles = ((uint32_t)n + kSortTile - 1) / kSortTile;
+  for (int p = 0; p < passes; p++) {
+    const int shift = p * kRadixBits;
+    k_radix_hist<<<tiles, kCtaThreads, 0, st>>>(ka, (uint32_t)n, shift, hist, tiles);
+    k_radix_scan<<<256, kCtaThreads, 0, st>>>(hist, tiles, digit_total);
+    k_radix_scatter<<<tiles, kCtaThreads, 0, st>>>(ka, va, kb, vb, (uint32_t)n, shift, hist, digit_total, tiles);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  k_na_starts<<<(unsigned)std::min<uint64_t>((nb + 256) / 256, 4096), 256, 0, st>>>(ka, n, nb, starts);
+  if (cudaMemcpyAsync(perm, va, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+    cudaGetLastError();
+    return si_fail_c(SI_EDEVICE, "si_block_sort_noalloc: copy of the order failed");
+  }
+  return cudaGetLastError() == cudaSuccess ? SI_OK : si_fail_c(SI_EDEVICE, "si_block_sort_noalloc: launch failed");
+}
