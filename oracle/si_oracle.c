@@ -422,10 +422,10 @@ static void g2p_one(float* p, const int32_t dims[3], const int32_t* grid, const 
         }
         v3 t = vscale(wt, gv);
         v = vadd(v, t);
-        /* B += outer3(t, dpos), the one fused multiply-add of the canonical order */
-        B.c[0] = V(fmaf(dpos.x, t.x, B.c[0].x), fmaf(dpos.x, t.y, B.c[0].y), fmaf(dpos.x, t.z, B.c[0].z));
-        B.c[1] = V(fmaf(dpos.y, t.x, B.c[1].x), fmaf(dpos.y, t.y, B.c[1].y), fmaf(dpos.y, t.z, B.c[1].z));
-        B.c[2] = V(fmaf(dpos.z, t.x, B.c[2].x), fmaf(dpos.z, t.y, B.c[2].y), fmaf(dpos.z, t.z, B.c[2].z));
+        /* B += outer3(t, dpos) (linalg.js outer3: column k = t * dpos_k), unfused */
+        B.c[0] = V(B.c[0].x + t.x * dpos.x, B.c[0].y + t.y * dpos.x, B.c[0].z + t.z * dpos.x);
+        B.c[1] = V(B.c[1].x + t.x * dpos.y, B.c[1].y + t.y * dpos.y, B.c[1].z + t.z * dpos.y);
+        B.c[2] = V(B.c[2].x + t.x * dpos.z, B.c[2].y + t.y * dpos.z, B.c[2].z + t.z * dpos.z);
       }
   m3 C;
   for (int j = 0; j < 3; j++) C.c[j] = vscale(4.0f, B.c[j]);

@@ -17,9 +17,7 @@
  *
  * Canonical f32 evaluation order. WGSL pins neither FMA contraction nor the reduction order of
  * matrix products, so this file fixes one order and the CUDA kernels follow it exactly:
- *   - every f32 operation is rounded on its own (built with -ffp-contract=off), with one exception:
- *     the G2P gather accumulates B += outer3(wt*gv, dpos) as fmaf(dpos_k, t_i, B_ki) (WGSL lets a
- *     compiler contract it; P2G, whose i32 sums must match bit for bit, has no fused operation);
+ *   - every f32 operation is rounded on its own (built with -ffp-contract=off; no fused operation);
  *   - binary expressions evaluate left to right as written in the WGSL;
  *   - mat*vec: r_i = (M0_i*v0 + M1_i*v1) + M2_i*v2 (columns Mk); mat*mat likewise per column;
  *   - dot(a,b) = (a0*b0 + a1*b1) + a2*b2; length = sqrt(dot); normalize(v) = v_i / length(v);
@@ -32,8 +30,10 @@
  * f32 sequence runs on both sides, the whole particle state agree with the CUDA path bit for bit.
  *
  * Parity pin: the reference holds no golden vectors and runs only as WGSL in a browser. Its own
- * WGSL source is executed by tests/golden/wgsl_exec.py to make the fixtures under tests/golden/,
- * and this oracle is checked against them (bit-exact for keys/starts/grid, tolerance for G2P).
+ * WGSL source is executed by tests/golden/wgsl_exec.py (IEEE f32, the same order as above) to make
+ * the fixtures under tests/golden/, and this oracle is checked against them: keys, starts, sorted
+ * records, P2G grid sums and the grid update bit for bit; G2P bit for bit in every field that does
+ * not pass through log/exp, and within WGSL's accuracy bound of log/exp in the others.
  */
 #ifndef SI_ORACLE_H
 #define SI_ORACLE_H

@@ -486,10 +486,10 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
         }
         const v3 t = vscale(wt, gv);
         v = vadd(v, t);
-        // B += outer3(t, dpos) with one fused multiply-add per entry (the oracle uses fmaf alike)
-        B.c[0] = V(__fmaf_rn(dpx, t.x, B.c[0].x), __fmaf_rn(dpx, t.y, B.c[0].y), __fmaf_rn(dpx, t.z, B.c[0].z));
-        B.c[1] = V(__fmaf_rn(dpy, t.x, B.c[1].x), __fmaf_rn(dpy, t.y, B.c[1].y), __fmaf_rn(dpy, t.z, B.c[1].z));
-        B.c[2] = V(__fmaf_rn(dpz, t.x, B.c[2].x), __fmaf_rn(dpz, t.y, B.c[2].y), __fmaf_rn(dpz, t.z, B.c[2].z));
+        // B += outer3(t, dpos): column k gains t * dpos_k, product and sum rounded separately
+        B.c[0] = V(B.c[0].x + t.x * dpx, B.c[0].y + t.y * dpx, B.c[0].z + t.z * dpx);
+        B.c[1] = V(B.c[1].x + t.x * dpy, B.c[1].y + t.y * dpy, B.c[1].z + t.z * dpy);
+        B.c[2] = V(B.c[2].x + t.x * dpz, B.c[2].y + t.y * dpz, B.c[2].z + t.z * dpz);
       }
     }
   }

@@ -1,0 +1,226 @@
+"""Makes the golden fixtures of tests/golden/ by executing the reference's own WGSL (TEST INFRASTRUCTURE).
+
+Run in a checkout that has the reference beside it:
+    python tests/golden/gen_golden.py /root/reference
+It reads src/physics/mpm.js and src/shaders/linalg.js, builds each MPM kernel the way the
+reference's Kernel class wraps it (src/core/kernel.js:83-104: `let wgi = wid.x + wid.y * nwg.x;
+let i = wgi * WG + lidx;` and the `i >= u.n` guard), with the template values of a device without
+subgroups and with 16 KB of workgroup memory (tileCap = (16384 - 512) / 16 = 992, mpm.js:302), and
+runs them with wgsl_exec on small seeded scenes. Inputs are built with oracle/host_ref.py (the
+reference's host JavaScript restated). The outputs are committed as .npz files; the tests never need
+the reference.
+"""
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [HERE, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")]
+import host_ref  # noqa: E402
+import wgsl_exec as W  # noqa: E402
+from conftest import mulberry32  # noqa: E402
+
+WG = 256
+TILE_CAP = 992
+PPT = 2
+
+
+def kernel_sources(ref):
+    mpm = open(os.path.join(ref, "src/physics/mpm.js")).read()
+    lin = open(os.path.join(ref, "src/shaders/linalg.js")).read()
+    mods = W.field_template(lin, "defineModule('linalg'", "code") + "\n" + W.field_template(mpm, "defineModule('mpm'", "code")
+
+    def tpl(expr):
+        if expr.startswith("sg ?"):
+            return "{"                    # the portable path (no subgroups)
+        return {"this.tileCap": str(TILE_CAP), "this.tileCap * 4": str(TILE_CAP * 4), "PPT": str(PPT)}[expr]
+
+    class Values(dict):
+        def __contains__(self, k):
+            return True
+
+        def __getitem__(self, k):
+            return tpl(k)
+
+    out = {}
+    for name in ("mpm-p2g", "mpm-grid", "mpm-g2p", "mpm-key", "mpm-reorder", "mpm-retime"):
+        anchor = f"name: '{name}'"
+        start = mpm.index(anchor)
+        nxt = mpm.find("ctx.kernel({", start)
+        seg = mpm[start: nxt if nxt > 0 else len(mpm)]
+        shared = W.substitute(W.field_template(mpm, anchor, "shared"), Values()) if "shared:" in seg else ""
+        code = W.substitute(W.field_template(mpm, anchor, "code"), Values())
+        out[name] = (shared, code)
+    return mods, out
+
+
+def compile_kernel(mods, shared, code, dims, guard):
+    consts = f"const WG = {WG}u;\nconst DIMS = vec3u({dims[0]}u, {dims[1]}u, {dims[2]}u);\n"
+    pre = "let i = wgi * WG + lidx;\n" + ("if (i >= u.n) { return; }\n" if guard else "")
+    ns = W.compile_module(consts + mods + "\n" + shared, pre + code)
+    return ns
+
+
+def particle_buffer(rec):
+    return W.Buffer(np.ascontiguousarray(rec, np.float32).copy(), "f32", 32,
+                    struct=["x", "v", "c0", "c1", "c2", "f0", "f1", "f2"])
+
+
+def scene_records(grid, shapes, substeps=8):
+    g = host_ref.geometry(grid)
+    dt = 1 / 60 / substeps
+    recs, mats, count = [], np.zeros((8, 12), np.float32), 0
+    for k, (shape, mat, vel) in enumerate(shapes):
+        pts = host_ref.sample_shape(shape, g["dx"] / 2, 0.6, count + 1)
+        recs.append(host_ref.make_records(pts, k, vel, g["dims"], g["dx"], [0, 0, 0], dt))
+        mats[k] = host_ref.material_row(mat)
+        count += len(pts)
+    return g, np.concatenate(recs), mats, dt
+
+
+def randomise(rec, seed, scale=1.0, deform=False):
+    R = mulberry32(seed)
+    for k in range(len(rec)):
+        for a in range(3):
+            rec[k, 4 + a] = (R() - 0.5) * 0.4 * scale
+        for c in range(3):
+            for a in range(3):
+                rec[k, 8 + 4 * c + a] = (R() - 0.5) * 0.2 * scale
+        for o in (11, 15, 19, 23, 27, 31):
+            rec[k, o] = (R() - 0.5) * 0.3 * scale
+        if deform:
+            for c in range(3):
+                for a in range(3):
+                    rec[k, 20 + 4 * c + a] = (1.0 if a == c else 0.0) + (R() - 0.5) * 0.3
+        rec[k, 7] = 1.0 + (R() - 0.5) * 0.2
+    return rec
+
+
+def p2g(kern, mods, rec, dims, mats, vol4, force_global):
+    shared, code = kern["mpm-p2g"]
+    ns = compile_kernel(mods, shared, code, dims, guard=False)
+    nodes = int(np.prod(dims))
+    grid = W.Buffer(np.zeros(nodes * 4, np.int32), "i32", 1)
+    groups = math.ceil(len(rec) / (WG * PPT))
+    W.dispatch(ns, groups, WG, {"P": particle_buffer(rec), "grid": grid, "MATS": W.Buffer(mats.reshape(24, 4).copy(), "f32", 4)},
+               {"n": np.uint32(len(rec)), "vol4": np.float32(vol4), "forceGlobal": np.uint32(1 if force_global else 0)})
+    return grid.arr.reshape(nodes, 4).copy()
+
+
+def grid_update(kern, mods, g, dims, gravity, cols, ncol):
+    shared, code = kern["mpm-grid"]
+    ns = compile_kernel(mods, shared, code, dims, guard=True)
+    nodes = int(np.prod(dims))
+    buf = W.Buffer(g.copy(), "i32", 4)
+    W.dispatch(ns, math.ceil(nodes / WG), WG, {"grid": buf, "COL": W.Buffer(cols.reshape(48, 4).copy(), "f32", 4)},
+               {"n": np.uint32(nodes), "gravity": W.Vec(np.array(gravity, np.float32)), "bound": np.float32(3.0),
+                "numColliders": np.uint32(ncol), "floorFriction": np.float32(0.4)})
+    return buf.arr.copy()
+
+
+def g2p(kern, mods, rec, dims, gv, mats):
+    shared, code = kern["mpm-g2p"]
+    ns = compile_kernel(mods, shared, code, dims, guard=True)
+    P = particle_buffer(rec)
+    W.dispatch(ns, math.ceil(len(rec) / WG), WG,
+               {"P": P, "GV": W.Buffer(gv.view(np.float32).copy(), "f32", 4), "MATS": W.Buffer(mats.reshape(24, 4).copy(), "f32", 4)},
+               {"n": np.uint32(len(rec)), "bound": np.float32(3.0), "vmax": np.float32(0.9)})
+    return P.arr.copy()
+
+
+def sort(kern, mods, rec, dims, num_blocks):
+    """_sort(), mpm.js:614-621: keys + atomic ranks, exclusive scan of the counts, reorder."""
+    shared, code = kern["mpm-key"]
+    ns = compile_kernel(mods, shared, code, dims, guard=True)
+    n = len(rec)
+    key = W.Buffer(np.zeros(n, np.uint32), "u32", 1)
+    rank = W.Buffer(np.zeros(n, np.uint32), "u32", 1)
+    cnt = W.Buffer(np.zeros(num_blocks + 1, np.uint32), "u32", 1)
+    W.dispatch(ns, math.ceil(n / WG), WG, {"P": particle_buffer(rec), "key": key, "rank": rank, "cnt": cnt},
+               {"n": np.uint32(n)})
+    counts = cnt.arr.copy()
+    starts = np.concatenate([[0], np.cumsum(counts[:-1])]).astype(np.uint32)   # Scan.run semantics, scan.js:288-306
+    shared, code = kern["mpm-reorder"]
+    ns = compile_kernel(mods, shared, code, dims, guard=True)
+    dst = particle_buffer(np.zeros_like(rec))
+    W.dispatch(ns, math.ceil(n / WG), WG, {"src": particle_buffer(rec), "dst": dst, "key": key, "rank": rank,
+                                            "start": W.Buffer(starts.copy(), "u32", 1)}, {"n": np.uint32(n)})
+    return key.arr.copy(), starts, dst.arr.copy()
+
+
+def main(ref):
+    mods, kern = kernel_sources(ref)
+    out = os.path.join(HERE)
+    # ---- P2G (tile and global paths) with randomised v, C, tau: tests/physics.test.js:6-17
+    g, rec, mats, dt = scene_records(16, [({"box": [[0.3, 0.3, 0.3], [0.62, 0.6, 0.55]]}, dict(kind=0, density=1, stiffness=1.0, viscosity=0.0), [0, 0, 0]),
+                                          ({"sphere": [[0.55, 0.5, 0.6], 0.1]}, dict(kind=1, density=1.2, stiffness=0.7, poisson=0.45), [0, 0, 0])])
+    rec = randomise(rec, 3)
+    vol4 = np.float32(4 * (1 / 2 ** 3))
+    g_tile = p2g(kern, mods, rec, g["dims"], mats, vol4, False)
+    g_glob = p2g(kern, mods, rec, g["dims"], mats, vol4, True)
+    assert np.array_equal(g_tile, g_glob), "the reference's tile and global paths disagree"
+    np.savez_compressed(os.path.join(out, "p2g.npz"), rec=rec, mats=mats, dims=np.array(g["dims"]), vol4=vol4, grid=g_tile)
+    print("p2g", rec.shape, int((g_tile[:, 3] != 0).sum()), "nodes")
+    # ---- grid update with walls, floor friction and three collider kinds
+    cols = np.zeros((16, 12), np.float32)
+    cl = [{"type": "sphere", "center": [0.45, 0.45, 0.45], "radius": 0.12, "velocity": [0.3, 0, 0], "friction": 0.5},
+          {"type": "box", "center": [0.6, 0.35, 0.5], "half": [0.08, 0.05, 0.1]},
+          {"type": "plane", "center": [0, 0.3, 0], "normal": [0.1, 1, 0]}]
+    for k, c in enumerate(cl):
+        cols[k] = host_ref.collider_row(c, g["dx"], [0, 0, 0], dt)
+    grav = [np.float32(0), np.float32((-9.81 * dt * dt) / g["dx"]), np.float32(0)]
+    gu = grid_update(kern, mods, g_tile, g["dims"], grav, cols, len(cl))
+    np.savez_compressed(os.path.join(out, "grid.npz"), grid_in=g_tile, dims=np.array(g["dims"]), gravity=np.array(grav),
+                        cols=cols, ncol=len(cl), grid_out=gu.reshape(-1, 4))
+    print("grid", int((gu != 0).any(1).sum()), "nodes")
+    # ---- G2P for water, honey, jelly, snow, sand from a deformed state
+    g2, rec2, mats2, _ = scene_records(16, [
+        ({"box": [[0.3, 0.3, 0.3], [0.45, 0.45, 0.45]]}, dict(kind=0, density=1, stiffness=1.0, viscosity=0.0), [0, 0, 0]),
+        ({"box": [[0.5, 0.3, 0.3], [0.62, 0.42, 0.42]]}, dict(kind=0, density=1.4, stiffness=0.9, viscosity=1.0), [0, 0, 0]),
+        ({"box": [[0.3, 0.5, 0.3], [0.42, 0.62, 0.42]]}, dict(kind=1, density=1, stiffness=0.35, poisson=0.3), [0, 0, 0]),
+        ({"box": [[0.5, 0.5, 0.3], [0.62, 0.62, 0.42]]}, dict(kind=2, density=0.4, stiffness=0.6, poisson=0.2, hardening=10, compression=0.025, stretch=0.0075), [0, 0, 0]),
+        ({"box": [[0.4, 0.4, 0.5], [0.52, 0.52, 0.62]]}, dict(kind=3, density=1.6, stiffness=0.6, poisson=0.3, friction=30), [0, 0, 0])])
+    rec2 = randomise(rec2, 7, scale=0.5, deform=True)
+    gsum = p2g(kern, mods, rec2, g2["dims"], mats2, vol4, False)
+    gv = grid_update(kern, mods, gsum, g2["dims"], grav, np.zeros((16, 12), np.float32), 0)
+    out2 = g2p(kern, mods, rec2, g2["dims"], gv, mats2)
+    np.savez_compressed(os.path.join(out, "g2p.npz"), rec=rec2, mats=mats2, dims=np.array(g2["dims"]), grid=gsum, gv=gv,
+                        gravity=np.array(grav), vol4=vol4, out=out2)
+    print("g2p", rec2.shape)
+    # ---- block sort of a stirred state
+    g3, rec3, mats3, _ = scene_records(32, [({"box": [[0.1, 0.1, 0.1], [0.4, 0.3, 0.35]]}, dict(kind=0, density=1, stiffness=1.0, viscosity=0.0), [0, 0, 0])])
+    rng = np.random.default_rng(5)
+    rec3 = rec3[rng.permutation(len(rec3))]
+    key, starts, dst = sort(kern, mods, rec3, g3["dims"], g3["num_blocks"])
+    np.savez_compressed(os.path.join(out, "sort.npz"), rec=rec3, dims=np.array(g3["dims"]), num_blocks=g3["num_blocks"],
+                        keys=key, starts=starts, sorted=dst)
+    print("sort", rec3.shape, g3["num_blocks"])
+    # ---- whole substeps in step()'s schedule (mpm.js:590-602): sort every 4th, P2G, grid, G2P.
+    # Water and honey only (no log/exp on their path), falling onto a sphere and a plane collider.
+    g4, rec4, mats4, dt4 = scene_records(16, [
+        ({"box": [[0.2, 0.35, 0.25], [0.5, 0.7, 0.6]]}, dict(kind=0, density=1, stiffness=1.0, viscosity=0.0), [0.5, -1.0, 0]),
+        ({"sphere": [[0.65, 0.6, 0.5], 0.12]}, dict(kind=0, density=1.4, stiffness=0.9, viscosity=1.0), [-0.5, 0, 0.3])])
+    cl4 = [{"type": "sphere", "center": [0.45, 0.25, 0.45], "radius": 0.1, "velocity": [0.2, 0, 0], "friction": 0.5},
+           {"type": "plane", "center": [0, 0.2, 0], "normal": [0.2, 1, 0]}]
+    cols4 = np.zeros((16, 12), np.float32)
+    for k, c in enumerate(cl4):
+        cols4[k] = host_ref.collider_row(c, g4["dx"], [0, 0, 0], dt4)
+    grav4 = [np.float32(0), np.float32((-9.81 * dt4 * dt4) / g4["dx"]), np.float32(0)]
+    K, P = 12, rec4.copy()
+    for s in range(K):
+        if s % 4 == 0:
+            _, _, P = sort(kern, mods, P, g4["dims"], g4["num_blocks"])
+        gs4 = p2g(kern, mods, P, g4["dims"], mats4, vol4, False)
+        gv4 = grid_update(kern, mods, gs4, g4["dims"], grav4, cols4, len(cl4))
+        P = g2p(kern, mods, P, g4["dims"], gv4, mats4)
+    np.savez_compressed(os.path.join(out, "trajectory.npz"), rec=rec4, mats=mats4, dims=np.array(g4["dims"]),
+                        num_blocks=g4["num_blocks"], cols=cols4, ncol=len(cl4), gravity=np.array(grav4), vol4=vol4,
+                        substeps=K, sort_every=4, out=P)
+    print("trajectory", rec4.shape, K)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

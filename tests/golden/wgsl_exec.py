@@ -44,6 +44,8 @@ def template_after(src, start):
             while depth:
                 if src[j] == "`":
                     _, j = template_after(src, j); continue
+                if src[j] in "'\"":                      # a quoted JS string: braces inside do not count
+                    j = src.index(src[j], j + 1) + 1; continue
                 if src[j] == "{":
                     depth += 1
                 elif src[j] == "}":
@@ -54,9 +56,12 @@ def template_after(src, start):
 
 
 def field_template(src, anchor, field):
-    """The template literal of `field: /* wgsl */ \`...\`` after the text `anchor`."""
+    """The template literal that follows `field:` (and an optional wgsl comment) after `anchor`."""
     a = src.index(anchor)
-    m = re.compile(field + r":\s*(/\*\s*wgsl\s*\*/\s*)?`").search(src, a)
+    m = re.compile(field + r":\s*(/\*\s*wgsl\s*\*/\s*)?([`'])").search(src, a)
+    if m.group(2) == "'":                       # a plain single-quoted string
+        end = src.index("'", m.end())
+        return src[m.end():end]
     return template_after(src, m.end() - 1)[0]
 
 
@@ -72,6 +77,8 @@ def substitute(tpl, values):
         while depth:
             if tpl[e] == "`":
                 _, e = template_after(tpl, e); continue
+            if tpl[e] in "'\"":
+                e = tpl.index(tpl[e], e + 1) + 1; continue
             depth += {"{": 1, "}": -1}.get(tpl[e], 0)
             e += 1
         expr = tpl[j + 2:e - 1].strip()
@@ -85,6 +92,7 @@ def substitute(tpl, values):
 
 class Vec:
     __slots__ = ("a",)
+    __array_ufunc__ = None          # numpy scalars defer to Vec's reflected operators
 
     def __init__(self, a):
         self.a = a
@@ -128,6 +136,8 @@ class Vec:
         self.a[int(k)] = v
 
     def __getattr__(self, name):
+        if not name or any(c not in "xyzwrgba" for c in name):
+            raise AttributeError(name)
         idx = ["xyzw".index(c) if c in "xyzw" else "rgba".index(c) for c in name]
         if len(idx) == 1:
             return self.a[idx[0]]
@@ -147,6 +157,7 @@ class Vec:
 class Mat:
     """3x3 f32, column-major: m[col][row]."""
     __slots__ = ("c",)
+    __array_ufunc__ = None
 
     def __init__(self, c):
         self.c = c   # (3, 3) float32, c[col, row]
@@ -182,6 +193,8 @@ def matvec(m, v):
 
 def wdiv(a, b):
     """WGSL `/`: float division, or integer division truncating toward zero."""
+    if isinstance(a, Vec) or isinstance(b, Vec):
+        return Vec(wdiv(a.a if isinstance(a, Vec) else a, b.a if isinstance(b, Vec) else b))
     if isinstance(a, (np.floating, float)) or isinstance(b, (np.floating, float)) or \
             (isinstance(a, np.ndarray) and a.dtype.kind == "f") or (isinstance(b, np.ndarray) and b.dtype.kind == "f"):
         return a / b
@@ -669,11 +682,13 @@ def compile_module(src, entry_body=None):
     structs = {it[1]: it[2] for it in items if it[0] == "struct"}
     g = Gen(structs)
     shared_decls = []
+    shared_names = {it[3] for it in items if it[0] == "decl" and it[2] == "workgroup"}
     for it in items:
         if it[0] == "fn":
             _, name, params, rt, body = it
             g.boxed = set()
             addressed(body, g.boxed)
+            g.boxed -= shared_names              # workgroup variables live in the namespace
             pnames = [p[0] for p in params]
             g.emit(f"def {name}({', '.join(pnames)}):", 0)
             for pn, pt in params:
@@ -692,7 +707,8 @@ def compile_module(src, entry_body=None):
         body = Parser("fn __main() {" + entry_body + "}").module()[0][4]
         g.boxed = set()
         addressed(body, g.boxed)
-        g.emit("def main():", 0)
+        g.boxed -= shared_names
+        g.emit("def main(lidx, wgi):", 0)
         g.stmts(body, 1)
         if not has_barrier(body):
             g.emit("yield", 1)    # every entry is a generator
@@ -720,9 +736,11 @@ def zero(ty):
         return Vec(np.zeros(int(name[3]), f32))
     if name == "array":
         inner, n = args
+        count = int(str(n).rstrip("iu"))
         if inner[0] == "atomic":
             dt = {"i32": i32, "u32": u32}[inner[1][0][0]]
-            return np.zeros(int(num_value(n[1]) if isinstance(n, tuple) and n[0] == "num" else n), dt)
+            return np.zeros(count, dt)
+        return np.zeros(count, {"i32": i32, "u32": u32, "f32": f32}[inner[0]])
     raise NotImplementedError(str(ty))
 
 
@@ -901,30 +919,20 @@ RUNTIME["f32"] = _conv(f32)
 # ============================================================================ dispatch
 
 def dispatch(ns, groups, wg, bindings, uniforms):
-    """Runs `groups` workgroups of `wg` invocations of ns['main'] with the given bindings."""
+    """Runs `groups` workgroups of `wg` invocations of ns['main'] with the given bindings. Within a
+    workgroup the invocations run in index order up to each barrier, then the next phase."""
     ns["u"] = types.SimpleNamespace(**uniforms)
     ns.update(bindings)
     main = ns["main"]
     for wgi in range(groups):
         for name, ty in ns["__shared_decls__"]:
             ns[name] = zero(ty)
-        gens = []
-        for lidx in range(wg):
-            ns_local = ns   # globals are shared; builtins of the invocation are set per step
-            gens.append((lidx, main))
-        live = []
-        for lidx, fn in gens:
-            ns["lidx"], ns["wgi"], ns["i"] = u32(lidx), u32(wgi), u32(wgi * wg + lidx)
-            it = fn()
-            live.append([lidx, it, False])
-        # run every invocation to its next barrier, in invocation order, until all finish
-        while any(not x[2] for x in live):
+        live = [[main(u32(lidx), u32(wgi)), False] for lidx in range(wg)]
+        while any(not x[1] for x in live):
             for x in live:
-                if x[2]:
+                if x[1]:
                     continue
-                ns["lidx"], ns["wgi"], ns["i"] = u32(x[0]), u32(wgi), u32(wgi * wg + x[0])
                 try:
-                    next(x[1])
+                    next(x[0])
                 except StopIteration:
-                    x[2] = True
-        del ns_local
+                    x[1] = True
