@@ -250,6 +250,188 @@ def run_ours(a, rank):
     return out
 
 
+# ----------------------------------------------------------------------------- batched and served forms
+BATCH_EDGES = (16, 32, 48, 64)
+BATCH_MATERIALS = ("water", "jelly", "snow", "sand")
+
+
+def scene_specs(n, seed):
+    """Scenes drawn as the batched workload: grid edge uniform in {16,32,48,64}, particle count
+    log-uniform in [2k, 260k] capped by 8 ppc of the interior (edge - 6)^3 cells, material uniform
+    over water/jelly/snow/sand, a box of that many cells at a random place, a random velocity."""
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for _ in range(n):
+        edge = rng.choice(BATCH_EDGES)
+        inner = edge - 6
+        target = min(math.exp(rng.uniform(math.log(2000), math.log(260000))), 8 * inner ** 3)
+        cells = target / 8
+        sx = sy = max(1, min(inner, round(cells ** (1 / 3))))
+        sz = max(1, min(inner, round(cells / (sx * sy))))
+        lo = [3 + rng.randrange(0, inner - d + 1) for d in (sx, sy, sz)]
+        vel = [rng.uniform(-1, 1), rng.uniform(-1, 0.5), rng.uniform(-1, 1)]
+        out.append({"edge": edge, "lo": lo, "size": [sx, sy, sz], "material": rng.choice(BATCH_MATERIALS),
+                    "vel": vel, "seed": rng.randrange(1, 1 << 30)})
+    return out
+
+
+def spec_capacity(s):
+    return 8 * (s["size"][0] + 1) * (s["size"][1] + 1) * (s["size"][2] + 1)
+
+
+def fill_scene(sim, s):
+    e = s["edge"]
+    sim.add({"box": [[x / e for x in s["lo"]], [(x + d) / e for x, d in zip(s["lo"], s["size"])]]},
+            material=s["material"], velocity=s["vel"], seed=s["seed"])
+    return sim
+
+
+def b_alg(sims):
+    """Algorithmic bytes of one substep of these scenes: 256 B per particle + 32 B per node."""
+    return sum(256 * s.count + 32 * s.numNodes for s in sims)
+
+
+def run_batched(a, log):
+    """256 scenes in one world: one launch per phase for all of them, CUDA graphs, autotuned; against
+    the same scenes each stepped alone (the plain single-scene path) one after another."""
+    from shaderintel_gb300 import MPM, World
+    from shaderintel_gb300.autotune import autotune
+    specs = scene_specs(a.batch_scenes, 4242)
+    world = World()
+    sims = [fill_scene(MPM(world, grid=s["edge"], maxParticles=spec_capacity(s), substeps=8), s) for s in specs]
+    n_total = sum(s.count for s in sims)
+    K = a.batch_substeps
+    tune = autotune(world, substeps=4, repeats=2)
+    log(f"batched: autotune chose {tune['particles_per_cta']}/{tune['tile_nodes']}/{tune['flush']}")
+    for _ in range(a.warmup):
+        world.step(K)
+    world.sync()
+    l0 = world.launches()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    world.mark(2)
+    for _ in range(a.batch_steps):
+        world.step(K)
+    world.mark(3)
+    ms = world.elapsed(2, 3)
+    clk = clocks.stop()
+    launches = world.launches() - l0
+    value = n_total * K * a.batch_steps / (ms / 1e3)
+    # the plain path: each scene alone, K substeps, scene after scene (warmed up the same way)
+    for _ in range(2):
+        for s in sims:
+            s.step(dt=s.substepDt, K=K)
+    world.mark(4)
+    for s in sims:
+        s.step(dt=s.substepDt, K=K)
+    world.mark(5)
+    plain_ms = world.elapsed(4, 5)
+    plain = n_total * K / (plain_ms / 1e3)
+    peak, peak_kind = load_peaks()
+    bytes_substep = b_alg(sims)
+    achieved = bytes_substep * K * a.batch_steps / (ms / 1e3) / 1e9
+    out = {"workload": f"batched: {len(sims)} scenes, edge in {{16,32,48,64}}, N log-uniform 2k-260k capped by "
+                       "8 ppc of the interior, water/jelly/snow/sand, random box placement (seed 4242), "
+                       f"{K} substeps per step",
+           "scenes": len(sims), "particles": n_total, "grid_nodes": sum(s.numNodes for s in sims),
+           "substeps_per_step": K, "steps": a.batch_steps, "ms_per_step": ms / a.batch_steps,
+           "value": value, "unit": "particle-substeps/s",
+           "plain_value": plain, "plain_ms_per_step": plain_ms, "vs_plain": value / plain,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "peak_source": peak_kind, "algorithmic_bytes_per_substep": bytes_substep},
+           "tuning": tune, "gpu_launches": launches, "clocks": clk,
+           "l2": f"inputs larger than L2 ({n_total * 128 / 1e6:.0f} MB particle state)"}
+    world.destroy()
+    return out
+
+
+def run_served(a, log):
+    """Continuous batching over up to `serve_resident` resident scenes drawn as the batched workload:
+    Poisson arrivals of step(dt, K) with K uniform in 1..32, admission by a 150 GB budget, scenes
+    retired after 500 substeps and replaced by new ones."""
+    import collections
+    import random
+    from shaderintel_gb300.serving import Server
+    rng = random.Random(77)
+    spec_iter = iter(scene_specs(1 << 20, 9191))
+    srv = Server(budget_bytes=150 * 10 ** 9)
+    peak, _ = load_peaks()
+    resident, given, outstanding = [], {}, collections.defaultdict(list)
+    retiring = []
+    refused = admitted = retired = 0
+
+    def admit_one():
+        nonlocal refused, admitted
+        s = next(spec_iter)
+        try:
+            sim = srv.admit(grid=s["edge"], maxParticles=spec_capacity(s), substeps=8)
+        except Exception:
+            refused += 1
+            return None
+        fill_scene(sim, s)
+        admitted += 1
+        given[sim] = 0
+        resident.append(sim)
+        return sim
+
+    for _ in range(a.serve_resident):
+        admit_one()
+    log(f"served: {len(resident)} resident scenes, {sum(s.count for s in resident)} particles")
+    srv.stats(reset=True)
+    t0 = time.perf_counter()
+    next_t = t0
+    n_sub = 0
+    bytes_done = 0
+    all_tickets = []
+    while True:
+        now = time.perf_counter()
+        if now - t0 >= a.serve_seconds:
+            break
+        if now < next_t:
+            time.sleep(min(next_t - now, 0.0005))
+            continue
+        next_t += rng.expovariate(a.serve_rate)
+        sim = resident[rng.randrange(len(resident))]
+        K = rng.randint(1, 32)
+        t = srv.submit(sim, K=K)
+        all_tickets.append(t)
+        outstanding[sim].append(t)
+        given[sim] += K
+        n_sub += K
+        bytes_done += K * (256 * sim.count + 32 * sim.numNodes)
+        if given[sim] >= 500:            # retire after 500 substeps: no more requests, then replace
+            resident.remove(sim)
+            retiring.append(sim)
+            admit_one()
+        for r in list(retiring):         # retire those whose last request has finished
+            done, _ = srv.poll(outstanding[r][-1])
+            if done:
+                outstanding[r].pop()
+                for tk in outstanding.pop(r):
+                    srv.wait(tk, timeout_ms=60000)
+                srv.retire(r)
+                retiring.remove(r)
+                retired += 1
+    for sim, tks in outstanding.items():
+        for tk in tks:
+            srv.wait(tk, timeout_ms=600000)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.destroy()
+    thr = st["particle_substeps"] / wall
+    return {"workload": f"served: Poisson arrivals {a.serve_rate:g}/s for {a.serve_seconds:g} s over up to "
+                        f"{a.serve_resident} resident scenes drawn as the batched workload, K uniform 1..32, "
+                        "150 GB admission budget, retire after 500 substeps",
+            "requests": st["requests_done"], "substeps": st["substeps_done"], "wall_s": wall,
+            "value": thr, "unit": "particle-substeps/s", "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+            "mean_ms": st["mean_ms"], "max_ms": st["max_ms"], "busy_s": st["busy_s"],
+            "admitted": admitted, "retired": retired, "refused": refused,
+            "roofline": {"bound": "hbm", "achieved": bytes_done / wall / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": bytes_done / wall / 1e9 / peak},
+            "resident_peak_bytes": st["resident_bytes"], "budget_bytes": st["budget_bytes"]}
+
+
 def traffic_per_launch(cfg):
     """DRAM bytes per k_g2p launch from the committed ncu summary, if one exists for this workload."""
     p = os.path.join(ROOT, "profiles", f"g2p_{cfg}_traffic.txt")
@@ -287,6 +469,14 @@ def main():
     p.add_argument("--config", choices=list(CONFIGS), default="mixed")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-batched", action="store_true", help="skip the batched-form leg")
+    p.add_argument("--batch-scenes", type=int, default=256)
+    p.add_argument("--batch-substeps", type=int, default=100)
+    p.add_argument("--batch-steps", type=int, default=3)
+    p.add_argument("--no-served", action="store_true", help="skip the served-form leg")
+    p.add_argument("--serve-seconds", type=float, default=10.0)
+    p.add_argument("--serve-rate", type=float, default=2000.0)
+    p.add_argument("--serve-resident", type=int, default=1000)
     a = p.parse_args()
     if a.warmup < 3:
         a.warmup = 3
@@ -299,6 +489,11 @@ def main():
             print(json.dumps(run_reference(a)))
         return
     out = run_ours(a, rank)
+    log = lambda m: print(m, file=sys.stderr, flush=True)   # noqa: E731
+    if world_size == 1 and not a.no_batched:
+        out["batched"] = run_batched(a, log)
+    if world_size == 1 and not a.no_served:
+        out["served"] = run_served(a, log)
     if world_size > 1:   # independent replicas: the job value is the sum, the time the max over ranks
         import torch.distributed as dist
         dist.init_process_group("gloo")

@@ -84,8 +84,12 @@ int si_world_set_graphs(si_world* w, int32_t enable); /* replay substeps from CU
 /* Per-phase GPU time in ms since the last reset: [sort, p2g, grid, g2p] — the labels
  * 'mpm sort' | 'mpm p2g' | 'mpm grid' | 'mpm g2p' of mpm.js:591-600. Timing is off until enabled. */
 int si_world_profile(si_world* w, int32_t enable, double ms_out[4], int32_t reset);
-/* Tuning knobs found by the autotuner: particles per CTA and tile capacity in nodes. */
-int si_world_set_tuning(si_world* w, int32_t particles_per_cta, int32_t tile_nodes);
+/* Tuning knobs chosen by the autotuner (shaderintel_gb300/autotune.py): particles per CTA (256, 512
+ * or 1024), the shared tile's capacity in nodes (a CTA whose stencils span more nodes uses the
+ * global path) and the P2G flush strategy (0: shared tile, non-zero nodes flushed with global i32
+ * atomics; 1: global i32 atomics per particle and node). Results are the same bits for every
+ * setting. No counterpart in the reference, whose tile capacity follows the device limit. */
+int si_world_set_tuning(si_world* w, int32_t particles_per_cta, int32_t tile_nodes, int32_t flush);
 /* Timing on the world's own stream (the reference times regions with GPU timestamps,
  * src/core/context.js:168-181): si_world_mark records event `slot` (0..7); si_world_elapsed waits
  * for mark b and returns the GPU time from mark a to mark b in ms. */

@@ -56,7 +56,7 @@ SIGNATURES = {
     "si_world_sync": (ctypes.c_int, [vp]),
     "si_world_set_graphs": (ctypes.c_int, [vp, ctypes.c_int32]),
     "si_world_profile": (ctypes.c_int, [vp, ctypes.c_int32, c_double_p, ctypes.c_int32]),
-    "si_world_set_tuning": (ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32]),
+    "si_world_set_tuning": (ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "si_world_mark": (ctypes.c_int, [vp, ctypes.c_int32]),
     "si_world_elapsed": (ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, c_double_p]),
     "si_world_launches": (ctypes.c_int, [vp, c_int64_p]),

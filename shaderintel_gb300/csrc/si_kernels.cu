@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
     // 4. P2G of the next substep through the same shared memory (cta_scatter synchronises first)
     if (fuse)
       cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
-                  reinterpret_cast<int*>(ts.grid_next), false, t.tile_nodes, tile, sbox);
+                  reinterpret_cast<int*>(ts.grid_next), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox);
     else
       cta_sync();
   }

@@ -244,6 +244,7 @@ static TickScene substep_entry(si_mpm* h) {
   const bool sort_now = h->sort_every > 0 && h->step_count % h->sort_every == 0;
   const bool next_sort = h->sort_every > 0 && (h->step_count + 1) % h->sort_every == 0;
   uint32_t f = F_FUSE;
+  if (h->w->flush) f |= F_FORCE_GLOBAL;
   if (!h->pending) { f |= F_P2G; if (!h->next_clear) f |= F_CLEAR; }
   if (sort_now) { f |= F_GATHER; if (!h->keys_valid) f |= F_KEYS_NOW; }
   if (next_sort) f |= F_KEYS;
@@ -370,7 +371,7 @@ static int run_plan(si_world* w, std::vector<HostTick>& plan) {
       off += k.ts.size() * sizeof(TickScene);
     }
   }
-  const bool graph_ok = w->use_graphs && !w->profile;
+  bool graph_ok = w->use_graphs && !w->profile;
   if (graph_ok) {
     for (auto& g : w->graphs) {
       if (same_plan(*g, plan, bytes, w)) {
@@ -380,6 +381,20 @@ static int run_plan(si_world* w, std::vector<HostTick>& plan) {
         return SI_OK;
       }
     }
+    // A plan is captured the second time it is seen; one that does not repeat (a serving round
+    // over a changing set of scenes) runs as direct launches and pays no capture.
+    uint64_t hsh = 1469598103934665603ull;
+    for (uint8_t b : bytes) hsh = (hsh ^ b) * 1099511628211ull;
+    hsh ^= ((uint64_t)w->ppt << 48) ^ ((uint64_t)plan.size() << 32) ^ (uint64_t)w->tile_nodes;
+    bool repeat = false;
+    for (uint64_t s : w->seen) repeat |= (s == hsh);
+    if (!repeat) {
+      w->seen[w->seen_next] = hsh;
+      w->seen_next = (w->seen_next + 1) % 16;
+      graph_ok = false;
+    }
+  }
+  if (graph_ok) {
     auto g = std::make_unique<GraphPlan>();
     CK(cudaMalloc((void**)&g->table, std::max<size_t>(bytes.size(), 16)));
     CK(cudaMemcpyAsync(g->table, bytes.data(), bytes.size(), cudaMemcpyHostToDevice, w->st));
@@ -583,11 +598,14 @@ int si_world_profile(si_world* w, int32_t enable, double ms_out[4], int32_t rese
   return SI_OK;
 }
 
-int si_world_set_tuning(si_world* w, int32_t particles_per_cta, int32_t tile_nodes) {
+int si_world_set_tuning(si_world* w, int32_t particles_per_cta, int32_t tile_nodes, int32_t flush) {
   GUARD_WORLD(w);
   if (particles_per_cta % kCtaThreads) return si_fail(SI_EINVAL, "particles per CTA must be a multiple of 256");
+  if (flush != 0 && flush != 1) return si_fail(SI_EINVAL, "flush strategy must be 0 (shared tile) or 1 (global)");
   CK(cudaStreamSynchronize(w->st));
-  return world_configure(w, particles_per_cta / kCtaThreads, tile_nodes);
+  int r = world_configure(w, particles_per_cta / kCtaThreads, tile_nodes);
+  if (!r) w->flush = flush;
+  return r;
 }
 
 int si_world_mark(si_world* w, int32_t slot) {

@@ -42,6 +42,7 @@ struct si_world {
   std::recursive_mutex api_mu;      // serialises API calls on this world with the server's rounds
   // tuning (autotuner: particles per CTA = 256 * ppt, shared tile capacity in nodes)
   int ppt = 1, tile_nodes = 2048;
+  int flush = 0;                    // P2G flush: 0 shared tile + non-zero node flush, 1 global atomics
   int ctas_p2g = 0, ctas_g2p = 0, ctas_grid = 0, ctas_misc = 0;
   // sort scratch (grown on demand)
   uint32_t *ka = nullptr, *va = nullptr, *kb = nullptr, *vb = nullptr;
@@ -56,6 +57,8 @@ struct si_world {
   bool use_graphs = true;
   std::vector<std::unique_ptr<GraphPlan>> graphs;
   uint64_t graph_clock = 0;
+  uint64_t seen[16] = {};           // hashes of recent plans: a plan is captured when it repeats
+  int seen_next = 0;
   // profiling: per-phase time [sort, p2g, grid, g2p]
   bool profile = false;
   double prof_ms[4] = {0, 0, 0, 0};

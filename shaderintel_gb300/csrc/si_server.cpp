@@ -114,32 +114,56 @@ static void server_loop(si_server* s) {
     K = std::max(K, 1);
     std::vector<si_mpm*> run;
     std::vector<double> dts;
+    std::vector<Request*> fin;   // the request that this round finishes, per scene (or null)
     auto* comp = new Completion{s, {}, 0, (int64_t)K};
     for (si_mpm* h : act) {
       Request* r = s->queues[h].front();
       r->remaining -= K;
+      fin.push_back(nullptr);
       if (r->remaining <= 0) {
         comp->reqs.push_back(r);
+        fin.back() = r;
         s->queues[h].pop_front();
       }
       run.push_back(h);
       dts.push_back(r->dt);
-      comp->particle_substeps += h->count * (int64_t)K;
     }
     lk.unlock();
     int err = SI_OK;
     {
       std::lock_guard<std::recursive_mutex> wg(w->api_mu);
+      {
+        // drop scenes retired since they were picked (retire destroys them only under api_mu);
+        // a request they would have finished ends as destroyed
+        std::lock_guard<std::mutex> g(s->mu);
+        size_t k = 0;
+        for (size_t i = 0; i < run.size(); i++) {
+          if (s->footprint.count(run[i])) {
+            run[k] = run[i]; dts[k] = dts[i]; k++;
+          } else if (fin[i]) {
+            fin[i]->status = SI_EDESTROYED;
+          }
+        }
+        run.resize(k);
+        dts.resize(k);
+      }
+      for (si_mpm* h : run) comp->particle_substeps += h->count * (int64_t)K;
       // requests carry their own dt: retime before the round when it changes (mpm.js:140-145)
       for (size_t i = 0; i < run.size() && !err; i++)
         if (dts[i] > 0 && dts[i] != run[i]->dt) err = si_mpm_set_substep_dt(run[i], dts[i]);
-      if (!err) err = run_substeps(w, run, K);
+      if (!err && !run.empty()) err = run_substeps(w, run, K);
       if (!err) {
-        std::lock_guard<std::mutex> g(s->mu);
-        if (s->inflight++ == 0) s->busy_since = Clock::now();
-        s->ticks += K;
+        {
+          std::lock_guard<std::mutex> g(s->mu);
+          if (s->inflight++ == 0) s->busy_since = Clock::now();
+          s->ticks += K;
+        }
+        if (cudaLaunchHostFunc(w->st, on_complete, comp) != cudaSuccess) {
+          std::lock_guard<std::mutex> g(s->mu);
+          if (--s->inflight == 0) s->busy_s += std::chrono::duration<double>(Clock::now() - s->busy_since).count();
+          err = si_fail(SI_EDEVICE, "cudaLaunchHostFunc failed");
+        }
       }
-      if (!err) cudaLaunchHostFunc(w->st, on_complete, comp);
     }
     lk.lock();
     if (err) {
@@ -236,23 +260,23 @@ int si_server_admit(si_server* s, const si_mpm_desc* desc, si_mpm** out) {
 int si_server_retire(si_server* s, si_mpm* h) {
   if (!s || !h) return si_fail(SI_EINVAL, "null argument");
   {
+    // The scene stops being resident first: a round that picked it before this point re-checks
+    // residency under the world's lock, which the destruction below also takes.
     std::lock_guard<std::mutex> g(s->mu);
     auto it = s->queues.find(h);
     if (it == s->queues.end()) return si_fail(SI_EINVAL, "not a resident scene of this server");
-    for (Request* r : it->second) fail_request(s, r, SI_EDESTROYED);   // none of these is on the device
-    it->second.clear();
+    for (Request* r : it->second) fail_request(s, r, SI_EDESTROYED);   // none of these finished
+    s->queues.erase(it);
+    s->resident -= s->footprint[h];
+    s->footprint.erase(h);
   }
-  // requests already on the device finish first: the scene is released on the server thread
+  s->cv_done.notify_all();
+  // substeps already enqueued are ordered before the stream-ordered release of the scene's memory
   run_on_world(s, [](void* p) {
     si_mpm* h = static_cast<si_mpm*>(p);
     h->served = false;
     si_mpm_destroy(h);
   }, h);
-  std::lock_guard<std::mutex> g(s->mu);
-  s->resident -= s->footprint[h];
-  s->footprint.erase(h);
-  s->queues.erase(h);
-  s->cv_done.notify_all();
   return SI_OK;
 }
 

@@ -121,8 +121,9 @@ class World:
         check(L.lib().si_world_profile(self._h, 1 if enable else 0, ms, 1 if reset else 0))
         return dict(zip(("mpm sort", "mpm p2g", "mpm grid", "mpm g2p"), list(ms)))
 
-    def set_tuning(self, particles_per_cta, tile_nodes):
-        check(L.lib().si_world_set_tuning(self._h, int(particles_per_cta), int(tile_nodes)))
+    def set_tuning(self, particles_per_cta=256, tile_nodes=2048, flush=0):
+        """Particles per CTA, shared tile capacity (nodes) and P2G flush strategy (0 tile, 1 global)."""
+        check(L.lib().si_world_set_tuning(self._h, int(particles_per_cta), int(tile_nodes), int(flush)))
 
     def mark(self, slot):
         """Record timing event `slot` (0..7) on the world's stream."""
@@ -406,6 +407,10 @@ class MPM:
 
     def destroy(self):
         if self.destroyed:
+            return
+        server = getattr(self, "_server", None)
+        if server is not None and server._h:
+            server.retire(self)   # a resident simulation leaves through its server
             return
         self.destroyed = True
         check(L.lib().si_mpm_destroy(self._h))
