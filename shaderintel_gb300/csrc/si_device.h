@@ -6,7 +6,10 @@
 //   grid:      two node arrays of int4 (ping-pong: P2G of substep s+1 is fused into the G2P of
 //              substep s and lands in the other array, which the grid update of s cleared);
 //   keys:      u32 per particle (block key of the last sort, pre-sort order, mpm.js:569);
-//   starts:    u32 x (num_blocks + 1) (mpm.js:122, after the scan).
+//   starts:    u32 x (num_blocks + 1) (mpm.js:122, after the scan);
+//   box:       i32 x 2 x 8: for each grid array, the box of the particle bases whose P2G filled it.
+//              A node outside the box of an array is zero there, so the grid update of a scene in
+//              steady stepping visits only box_cur + box_next (+ the stencil reach), not the grid.
 // A tick is one substep of every scene that has work. The host builds one TickScene per such
 // scene; kernels map a flat chunk index to its scene by binary search over the chunk prefixes.
 #pragma once
@@ -31,6 +34,7 @@ constexpr uint32_t F_FORCE_GLOBAL = 16u; // P2G skips the shared-memory tile (mp
 constexpr uint32_t F_NO_CLEAR_NEXT = 32u; // grid update leaves grid_next alone
 constexpr uint32_t F_KEYS_NOW = 64u;  // compute the block keys of the current positions before the sort
 constexpr uint32_t F_CLEAR = 128u;    // zero `grid` before the standalone P2G
+constexpr uint32_t F_BOXED = 256u;    // grid update: nodes outside box_cur + box_next are zero in both arrays
 
 struct SceneParams {             // per scene, device resident, rewritten when a value changes
   float4 mats[24];               // 8 materials x 3 vec4 (mpm.js:116)
@@ -51,6 +55,8 @@ struct TickScene {               // per tick and active scene, host built
   float4* Palt;                  // destination of the sort's gather
   int4* grid;                    // grid of this substep
   int4* grid_next;               // grid of the next substep
+  int32_t* box_cur;              // stencil-base box (min xyz, max xyz) of the P2G that filled `grid`
+  int32_t* box_next;             // the same for `grid_next` (the fused P2G of this substep adds to it)
   uint32_t* keys;                // per-scene key array (pre-sort order)
   uint32_t* starts;              // per-scene starts (num_blocks + 1)
   int64_t cap;                   // stream stride in float4
@@ -85,6 +91,7 @@ struct SortInfo {                // one tick's sort
 void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_clear(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st);
+void launch_box_reset(const TickInfo& t, cudaStream_t st);
 void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
 void launch_reorder(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
 void launch_keys(const TickInfo& t, int grid_ctas, cudaStream_t st);

@@ -231,7 +231,7 @@ __device__ __forceinline__ void scat_load(const float* sc, int chunk, int slot, 
 // `reg` (one per thread, valid if has_reg) when sc == nullptr, else from the `count` staged copies.
 __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const float* sc, int chunk, int count,
                                             const int32_t* dims, int* __restrict__ grid, bool force_global,
-                                            int tile_nodes, int* tile, int* sbox) {
+                                            int tile_nodes, int* tile, int* sbox, int32_t* scene_box) {
   constexpr int tile_cap = kTileNodes;
   const int tid = threadIdx.x;
   if (tid < 3) { sbox[tid] = 0x3fffffff; sbox[3 + tid] = -0x3fffffff; }
@@ -260,6 +260,10 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
   cta_sync();
   const int o0 = sbox[0], o1 = sbox[1], o2 = sbox[2];
   const int ex = sbox[3] - o0 + 3, ey = sbox[4] - o1 + 3, ez = sbox[5] - o2 + 3;
+  if (tid == 0 && scene_box != nullptr && ex > 0) {   // the scene's box of P2G bases (grid update bounds)
+    atomicMin(&scene_box[0], o0); atomicMin(&scene_box[1], o1); atomicMin(&scene_box[2], o2);
+    atomicMax(&scene_box[3], sbox[3]); atomicMax(&scene_box[4], sbox[4]); atomicMax(&scene_box[5], sbox[5]);
+  }
   cta_sync();   // sbox is reused by the next chunk
   if (ex <= 0 || ey <= 0 || ez <= 0) return;    // no valid particle in the chunk
   const long long tn = (long long)ex * ey * ez;
@@ -332,7 +336,8 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t
       if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + threadIdx.x, reg);
     }
     cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
-                reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox);
+                reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox,
+                ts.box_cur);
   }
 }
 
@@ -376,27 +381,55 @@ __device__ __forceinline__ float collider_sdf(uint32_t kind, v3 d, float4 s) {
   return vdot(d, V(s.x, s.y, s.z));
 }
 
+// The nodes a scene's grid update visits: the whole grid, or with F_BOXED the nodes under the
+// stencils of box_cur + box_next (bases lo..hi reach nodes lo..hi+2), clipped to the grid. Outside it
+// both arrays are zero (never scattered to, or cleared since), so the update writes nothing there.
+struct NodeRegion {
+  int32_t x0, y0, z0, nx, ny, nz;
+};
+__device__ __forceinline__ NodeRegion grid_region(const TickScene& ts, const int32_t* d) {
+  NodeRegion r{0, 0, 0, d[0], d[1], d[2]};
+  if (ts.flags & F_BOXED) {
+    int32_t lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      lo[a] = max(0, min(ts.box_cur[a], ts.box_next[a]));
+      hi[a] = min(d[a], max(ts.box_cur[3 + a], ts.box_next[3 + a]) + 3);
+      if (hi[a] < lo[a]) hi[a] = lo[a];
+    }
+    r = NodeRegion{lo[0], lo[1], lo[2], hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  }
+  return r;
+}
+
 __global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
   for (uint32_t chunk = blockIdx.x; chunk < t.nchunks; chunk += gridDim.x) {
     const TickScene& ts = t.ts[find_scene_n(t.ts, t.nscenes, chunk)];
     const SceneParams* prm = ts.prm;
     const int64_t X = prm->dims[0], Y = prm->dims[1];
-    const int64_t nodes = X * Y * prm->dims[2];
+    const NodeRegion reg = grid_region(ts, prm->dims);
+    const uint32_t rxy = (uint32_t)reg.nx * (uint32_t)reg.ny;
+    const int64_t nodes = (int64_t)rxy * reg.nz;
     const int64_t first = (int64_t)(chunk - ts.nchunk_begin) * kNodeChunk;
+    if (first >= nodes) continue;
     const int64_t last = min(first + (int64_t)kNodeChunk, nodes);
     const float bound = prm->bound, ff = prm->floor_friction;
     const float g0 = prm->gravity[0], g1 = prm->gravity[1], g2 = prm->gravity[2];
     const v3 hi = V((float)prm->dims[0] - bound, (float)prm->dims[1] - bound, (float)prm->dims[2] - bound);
     const int ncol = prm->ncol;
     const bool clear_next = !(ts.flags & F_NO_CLEAR_NEXT);
-    for (int64_t i = first + threadIdx.x; i < last; i += blockDim.x) {
+    for (int64_t r = first + threadIdx.x; r < last; r += blockDim.x) {
+      const uint32_t lz = (uint32_t)r / rxy, rem = (uint32_t)r - lz * rxy;
+      const uint32_t ly = rem / (uint32_t)reg.nx, lx = rem - ly * (uint32_t)reg.nx;
+      const int64_t nxi = reg.x0 + lx, nyi = reg.y0 + ly, nzi = reg.z0 + lz;
+      const int64_t i = nxi + X * (nyi + Y * nzi);
       int4 g = ts.grid[i];
       float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (g.w > 0) {
         const float inv = 1.0f / 4194304.0f;
         float m = (float)g.w * inv;
         v3 v = V(((float)g.x * inv) / m + g0, ((float)g.y * inv) / m + g1, ((float)g.z * inv) / m + g2);
-        v3 c = V((float)(i % X), (float)((i / X) % Y), (float)(i / (X * Y)));
+        v3 c = V((float)nxi, (float)nyi, (float)nzi);
         if (c.y < bound && v.y < 0.0f) {
           float vn = -v.y;
           v.y = 0.0f;
@@ -437,8 +470,19 @@ __global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
         }
         out = make_float4(v.x, v.y, v.z, m);
       }
-      reinterpret_cast<float4*>(ts.grid)[i] = out;
+      if ((g.x | g.y | g.z | g.w) != 0) reinterpret_cast<float4*>(ts.grid)[i] = out;   // zero stays zero
       if (clear_next) ts.grid_next[i] = make_int4(0, 0, 0, 0);
+    }
+  }
+}
+
+// Empties box_next of every scene of the tick: the fused P2G of the G2P that follows rebuilds it.
+__global__ void k_box_reset(TickInfo t) {
+  for (int s = threadIdx.x; s < t.nscenes; s += blockDim.x) {
+    int32_t* b = t.ts[s].box_next;
+    if (b) {
+      b[0] = b[1] = b[2] = 0x3fffffff;
+      b[3] = b[4] = b[5] = -0x3fffffff;
     }
   }
 }
@@ -464,10 +508,11 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
 #pragma unroll 1
   for (int a = 0; a < 3; a++) {
     const float dpx = (float)a - f0;
+    const float wxa = a == 0 ? wx[0] : (a == 1 ? wx[1] : wx[2]);   // select, not a local-memory index
 #pragma unroll
     for (int b = 0; b < 3; b++) {
       const float dpy = (float)b - f1;
-      const float wab = wx[a] * wy[b];
+      const float wab = wxa * wy[b];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const float dpz = (float)c - f2;
@@ -707,7 +752,8 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
     // 4. P2G of the next substep through the same shared memory (cta_scatter synchronises first)
     if (fuse)
       cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
-                  reinterpret_cast<int*>(ts.grid_next), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox);
+                  reinterpret_cast<int*>(ts.grid_next), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox,
+                  ts.box_next);
     else
       cta_sync();
   }
@@ -814,6 +860,9 @@ void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st) {
   if (t.nchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.nchunks, (uint32_t)grid_ctas);
   k_grid<<<ctas, kCtaThreads, 0, st>>>(t);
+}
+void launch_box_reset(const TickInfo& t, cudaStream_t st) {
+  if (t.nscenes > 0) k_box_reset<<<1, kCtaThreads, 0, st>>>(t);
 }
 void launch_keys(const TickInfo& t, int grid_ctas, cudaStream_t st) {
   if (t.pchunks == 0) return;

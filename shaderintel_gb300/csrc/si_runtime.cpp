@@ -62,7 +62,7 @@ static uint32_t num_blocks_for(const int32_t d[3]) {
 
 static int64_t scene_footprint(int64_t cap, int64_t nodes, uint32_t nb) {
   return 2 * (int64_t)kStreams * 16 * cap + 2 * 16 * nodes + 4 * cap + 4 * ((int64_t)nb + 1) +
-         (int64_t)sizeof(SceneParams);
+         (int64_t)sizeof(SceneParams) + 64;
 }
 
 int64_t scene_footprint_of(const si_mpm_desc* in) {
@@ -173,6 +173,7 @@ static void invalidate(si_mpm* h) {
   if (h->pending) h->next_clear = false;
   h->pending = false;
   h->keys_valid = false;
+  h->box_ok = 0;
 }
 
 // ------------------------------------------------------------------ ticks
@@ -241,6 +242,8 @@ static TickScene substep_entry(si_mpm* h) {
   TickScene t = base_entry(h);
   t.grid = h->grid[1 - h->gcur];
   t.grid_next = h->grid[h->gcur];
+  t.box_cur = h->box + 8 * (1 - h->gcur);
+  t.box_next = h->box + 8 * h->gcur;
   const bool sort_now = h->sort_every > 0 && h->step_count % h->sort_every == 0;
   const bool next_sort = h->sort_every > 0 && (h->step_count + 1) % h->sort_every == 0;
   uint32_t f = F_FUSE;
@@ -248,6 +251,10 @@ static TickScene substep_entry(si_mpm* h) {
   if (!h->pending) { f |= F_P2G; if (!h->next_clear) f |= F_CLEAR; }
   if (sort_now) { f |= F_GATHER; if (!h->keys_valid) f |= F_KEYS_NOW; }
   if (next_sort) f |= F_KEYS;
+  // both boxes are exact once two standard substeps ran in a row: box_cur from the P2G that filled
+  // `grid` (the previous G2P, or the standalone P2G of a substep that started after box_ok was
+  // reset), box_next from the one before, whose grid update left values only inside it
+  if (h->box_ok >= 2) f |= F_BOXED;
   t.flags = f;
   // state after the substep
   h->gcur = 1 - h->gcur;
@@ -256,6 +263,7 @@ static TickScene substep_entry(si_mpm* h) {
   h->next_clear = false;
   h->keys_valid = next_sort;
   h->step_count++;
+  h->box_ok = std::min(h->box_ok + 1, 2);
   return t;
 }
 
@@ -292,6 +300,7 @@ static int64_t tick_kernels(const HostTick& k) {
   if (k.any_clear) n++;
   if (k.any_p2g) n++;
   if (k.mode == T_SUBSTEP || k.mode == T_GRID) n++;
+  if (k.mode == T_SUBSTEP) n++;   // box reset
   if (k.mode == T_SUBSTEP || k.mode == T_G2P) n++;
   return n;
 }
@@ -323,6 +332,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   if (k.any_p2g) launch_p2g(t, w->ctas_p2g, st);
   if (profile) cudaEventRecord(w->pev[2], st);
   if (k.mode == T_SUBSTEP || k.mode == T_GRID) launch_grid(t, w->ctas_grid, st);
+  if (k.mode == T_SUBSTEP) launch_box_reset(t, st);   // box_next starts empty for the fused P2G
   if (profile) cudaEventRecord(w->pev[3], st);
   if (k.mode == T_SUBSTEP || k.mode == T_G2P) launch_g2p(t, perm, w->ctas_g2p, st);
   if (profile) {
@@ -484,6 +494,10 @@ static int run_phase(si_mpm* h, int mode, uint32_t extra_flags) {
   TickScene t = base_entry(h);
   t.grid = h->grid[h->gcur];
   t.grid_next = h->grid[1 - h->gcur];
+  t.box_cur = h->box + 8 * h->gcur;
+  t.box_next = h->box + 8 * (1 - h->gcur);
+  h->box_ok = 0;   // a phase run by itself leaves the arrays as the reference does: the next substeps
+                   // visit the whole grid until both boxes are known again
   switch (mode) {
     case T_P2G: t.flags = F_P2G | F_CLEAR | extra_flags; break;
     case T_GRID: t.flags = F_NO_CLEAR_NEXT; break;
@@ -541,12 +555,13 @@ static void scene_release(si_mpm* h) {
   si_world* w = h->w;
   h->destroyed = true;
   for (void* p : {(void*)h->pbuf[0], (void*)h->pbuf[1], (void*)h->grid[0], (void*)h->grid[1], (void*)h->keys,
-                  (void*)h->starts, (void*)h->prm})
+                  (void*)h->starts, (void*)h->prm, (void*)h->box})
     if (p) cudaFreeAsync(p, w->st);
   h->pbuf[0] = h->pbuf[1] = nullptr;
   h->grid[0] = h->grid[1] = nullptr;
   h->keys = h->starts = nullptr;
   h->prm = nullptr;
+  h->box = nullptr;
   w->scenes.erase(std::remove(w->scenes.begin(), w->scenes.end(), h), w->scenes.end());
   world_free_graphs(w);
 }
@@ -694,6 +709,12 @@ int scene_create(si_world* w, const si_mpm_desc* in, si_mpm** out, bool own_worl
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->keys, std::max<size_t>(4 * (size_t)h->cap, 16), st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->starts, 4 * ((size_t)h->num_blocks + 1), st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->prm, sizeof(SceneParams), st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->box, 64, st);
+  if (e == cudaSuccess) {
+    static const int32_t empty[16] = {0x3fffffff, 0x3fffffff, 0x3fffffff, -0x3fffffff, -0x3fffffff, -0x3fffffff, 0, 0,
+                                      0x3fffffff, 0x3fffffff, 0x3fffffff, -0x3fffffff, -0x3fffffff, -0x3fffffff, 0, 0};
+    e = cudaMemcpyAsync(h->box, empty, sizeof(empty), cudaMemcpyHostToDevice, st);
+  }
   for (int b = 0; b < 2 && e == cudaSuccess; b++) e = cudaMemsetAsync(h->grid[b], 0, (size_t)h->nodes * 16, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->starts, 0, 4 * ((size_t)h->num_blocks + 1), st);
   if (e != cudaSuccess) {

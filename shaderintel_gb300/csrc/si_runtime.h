@@ -90,6 +90,8 @@ struct si_mpm {
   int gcur = 0;                     // grid of the last substep
   uint32_t* keys = nullptr;
   uint32_t* starts = nullptr;
+  int32_t* box = nullptr;           // [2][8]: stencil-base box of the P2G that filled grid[0] / grid[1]
+  int box_ok = 0;                   // standard substeps in a row (>= 2: both boxes describe the arrays)
   si::SceneParams* prm = nullptr;
   bool prm_dirty = true;
   bool pending = false;             // grid[1-gcur] holds the P2G of the current particle state
