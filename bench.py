@@ -432,6 +432,47 @@ def run_served(a, log):
             "resident_peak_bytes": st["resident_bytes"], "budget_bytes": st["budget_bytes"]}
 
 
+def run_conservation(substeps=200):
+    """The correctness gates reported beside the throughput: the 32^3 dam break (32,768 particles)
+    stepped `substeps` substeps through the same library; particle count and particle mass are
+    exact, the grid's fixed-point mass after P2G is compared with the particles' mass, and the
+    momentum sum and the energy (kinetic + gravitational, lattice units) are reported at the start
+    and the end."""
+    import numpy as np
+    from shaderintel_gb300 import World
+    world = World()
+    sim = build_gpu("dam_break", world)
+    rows = np.stack(sim._rows)
+    g = sim.gravity[1] * sim.substepDt ** 2 / sim.dx            # cells / substep^2
+
+    def state():
+        P = sim.readParticles()
+        m = rows[P.view(np.uint32)[:, 3] & 7, 1].astype(np.float64)
+        v = P[:, 4:7].astype(np.float64)
+        y = P[:, 1].astype(np.float64)
+        sim.p2g()
+        grid_mass = float(sim.readGrid()[:, 3].astype(np.int64).sum()) / 4194304.0
+        return {"particles": len(P), "mass": float(m.sum()), "grid_mass": grid_mass,
+                "momentum": (m[:, None] * v).sum(0).tolist(),
+                "energy": float((0.5 * m * (v * v).sum(1)).sum() - (m * g * y).sum())}
+
+    s0 = state()
+    devs = [abs(s0["grid_mass"] / s0["mass"] - 1)]
+    frames = substeps // sim.substeps
+    for _ in range(frames):
+        sim.step()
+        devs.append(abs(state()["grid_mass"] / s0["mass"] - 1))
+    s1 = state()
+    world.destroy()
+    return {"workload": CONFIGS["dam_break"]["desc"] + f", {frames * 8} substeps",
+            "particles_start": s0["particles"], "particles_end": s1["particles"],
+            "particle_mass": s0["mass"], "particle_mass_end": s1["mass"],
+            "grid_mass_rel_dev_max": max(devs),
+            "momentum_start": s0["momentum"], "momentum_end": s1["momentum"],
+            "energy_start": s0["energy"], "energy_end": s1["energy"],
+            "energy_drift_rel": (s1["energy"] - s0["energy"]) / abs(s0["energy"]) if s0["energy"] else None}
+
+
 def traffic_per_launch(cfg):
     """DRAM bytes per k_g2p launch from the committed ncu summary, if one exists for this workload."""
     p = os.path.join(ROOT, "profiles", f"g2p_{cfg}_traffic.txt")
@@ -494,6 +535,8 @@ def main():
         out["batched"] = run_batched(a, log)
     if world_size == 1 and not a.no_served:
         out["served"] = run_served(a, log)
+    if world_size == 1:
+        out["conservation"] = run_conservation()
     if world_size > 1:   # independent replicas: the job value is the sum, the time the max over ranks
         import torch.distributed as dist
         dist.init_process_group("gloo")

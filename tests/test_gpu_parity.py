@@ -270,6 +270,27 @@ def test_dam_break_reference():
     sim.destroy()
 
 
+def test_conservation_over_200_substeps():
+    """tests/physics.test.js:6-32 (mass within 1e-4, bounded momentum), over 200 substeps of the
+    32^3 dam break: particle count and mass exact, the grid's fixed-point mass after P2G within
+    1e-5 of the particles' mass at every frame, momentum and energy finite."""
+    sim = MPM(grid=32, maxParticles=40000, substeps=8)
+    sim.add({"box": [[3 / 32] * 3, [19 / 32] * 3]}, material="water")
+    n0 = sim.count
+    mass = float(sim._rows[0][1]) * n0
+    for frame in range(25):
+        sim.step()
+        P = sim.readParticles()
+        assert len(P) == n0 and np.isfinite(P).all()
+        sim.p2g()
+        grid_mass = float(sim.readGrid()[:, 3].astype(np.int64).sum()) / 4194304.0
+        assert abs(grid_mass / mass - 1) < 1e-5
+        v = P[:, 4:7].astype(np.float64)
+        assert np.abs(v).max() <= 0.9 + 1e-6              # vmax clamp, mpm.js:531
+    assert sim.stepCount == 200
+    sim.destroy()
+
+
 def test_retime_keeps_physical_speed():
     """tests/lifecycle.test.js:294-307."""
     def speed(substeps):
