@@ -192,6 +192,24 @@ int si_collider_row(const si_mpm* h, int32_t type, const double center[3], const
                     double radius, double friction, const double velocity[3], double substep_dt,
                     float row[12]);
 
+/* ---------------------------------------------------------------- fluid <-> rigid coupling
+ * MPM.couple(world, o) / uncouple() (mpm.js:244-259, src/physics/coupling.js:62-222): rigid bodies
+ * become moving boundaries of the grid. `bodies` is n records of 48 floats, the reference's Body
+ * (src/physics/rigid-wgsl.js:20-33: x (w = bounding radius), q, v, w, x0, q0, y, qy, size (w = shape
+ * 0 sphere / 1 box / 2 capsule), mass (x = m, 0 = static), props, info (4 u32 bit patterns: group,
+ * mask, flags, user)), in world units. Every substep the pass runs after the grid update with the
+ * bodies extrapolated by v (s + 0.5) dt, s the substep's index in its step() call
+ * (coupling.substep, mpm.js:596). n = 0 uncouples. friction 0.2, band 0.5 cells, mask all bits and
+ * density_scale 1 are the reference's defaults. */
+int si_mpm_couple(si_mpm* h, const float* bodies, int32_t n, double friction, double band, uint32_t mask,
+                  double density_scale);
+/* The rigid world moved: new body records (same count) for the next substeps (the B buffer). */
+int si_mpm_set_bodies(si_mpm* h, const float* bodies, int32_t n);
+/* coupling.finish() (coupling.js:199-206, mpm-rigid-apply): the reaction impulses summed since the
+ * last read, in world units, n x 8 floats (J xyz, 0, L xyz, 0) — what the reference adds to the
+ * rigid world's external impulses; the sums restart from zero. */
+int si_mpm_read_impulses(si_mpm* h, float* out, int32_t n);
+
 /* ---------------------------------------------------------------- serving
  * A request loop that keeps every scene resident in HBM and runs step(dt, K) requests by
  * continuous batching: each tick is one substep of every scene with work left; requests that

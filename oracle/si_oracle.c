@@ -536,6 +536,155 @@ void sio_retime(float* P, int64_t n, float k) {
   }
 }
 
+/* ------------------------------------------------------------------ coupling, coupling.js:31-196 */
+#define SIO_MAXC 128          /* MAX_CAND, coupling.js:25 */
+#define SIO_FPJ 16384.0f      /* coupling.js:26 */
+#define SIO_FPL 1024.0f       /* coupling.js:27 */
+#define SIO_F_SENSOR 2u       /* rigid-wgsl.js:35-36 */
+#define SIO_F_DISABLED 4u
+
+/* qmat, src/shaders/math.js:56-62 (columns) */
+static m3 qmat(const float* q) {
+  const float x = q[0], y = q[1], z = q[2], w = q[3];
+  m3 r;
+  r.c[0] = V(1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + w * z), 2.0f * (x * z - w * y));
+  r.c[1] = V(2.0f * (x * y - w * z), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + w * x));
+  r.c[2] = V(2.0f * (x * z + w * y), 2.0f * (y * z - w * x), 1.0f - 2.0f * (x * x + y * y));
+  return r;
+}
+static inline float wsign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+/* i32(e) of WGSL: truncation, saturating at the range ends, NaN -> 0 */
+static inline int32_t wgsl_i32(float x) {
+  if (x != x) return 0;
+  if (x >= 2147483648.0f) return 2147483647;
+  if (x <= -2147483648.0f) return (int32_t)(-2147483647 - 1);
+  return (int32_t)x;
+}
+
+/* bodySDF, coupling.js:31-58: signed distance from p to body b centred at c and the outward normal */
+static void body_sdf(const float* b, v3 c, v3 p, float* dist, v3* nrm) {
+  const uint32_t s = (uint32_t)(b[35] + 0.5f);            /* shapeOf, rigid-wgsl.js:75 */
+  const m3 R = qmat(b + 4);
+  const v3 lp = mv(mT(R), vsub(p, c));
+  if (s == 0u) {
+    const float d = vlen(lp);
+    const float m = fmaxf(d, 1e-6f);
+    *dist = d - b[32];
+    *nrm = mv(R, V(lp.x / m, lp.y / m, lp.z / m));
+    return;
+  }
+  if (s == 2u) {
+    const float h = b[33];
+    const v3 q = V(lp.x, lp.y - clampf(lp.y, -h, h), lp.z);
+    const float d = vlen(q);
+    const float m = fmaxf(d, 1e-6f);
+    const v3 t = V(q.x / m, q.y / m, q.z / m);
+    *dist = d - b[32];
+    *nrm = mv(R, d > 1e-6f ? t : V(0.0f, wsign(lp.y), 0.0f));
+    return;
+  }
+  const v3 h = V(b[32], b[33], b[34]);
+  const v3 q = V(fabsf(lp.x) - h.x, fabsf(lp.y) - h.y, fabsf(lp.z) - h.z);
+  if (q.x > 0.0f || q.y > 0.0f || q.z > 0.0f) {
+    const v3 dv = V(lp.x - clampf(lp.x, -h.x, h.x), lp.y - clampf(lp.y, -h.y, h.y), lp.z - clampf(lp.z, -h.z, h.z));
+    const float d = vlen(dv);
+    const float m = fmaxf(d, 1e-9f);
+    *dist = d;
+    *nrm = mv(R, V(dv.x / m, dv.y / m, dv.z / m));
+    return;
+  }
+  int ax = 0;
+  if (q.y > vget(q, ax)) ax = 1;
+  if (q.z > vget(q, ax)) ax = 2;
+  const float sg = vget(lp, ax) >= 0.0f ? 1.0f : -1.0f;
+  *dist = vget(q, ax);
+  *nrm = mv(R, V(ax == 0 ? sg : 0.0f, ax == 1 ? sg : 0.0f, ax == 2 ? sg : 0.0f));
+}
+
+void sio_couple(int32_t* grid, const int32_t dims[3], const float* bodies, int32_t n,
+                const sio_couple_params* p, int32_t* acc) {
+  const int32_t tiles[3] = {(dims[0] + 3) / 4, (dims[1] + 3) / 4, (dims[2] + 3) / 4};
+  const v3 origin = V(p->origin[0], p->origin[1], p->origin[2]);
+  int32_t cand[SIO_MAXC];
+  int32_t accj[SIO_MAXC * 3], accl[SIO_MAXC * 3];
+  for (int32_t tz = 0; tz < tiles[2]; tz++)
+    for (int32_t ty = 0; ty < tiles[1]; ty++)
+      for (int32_t tx = 0; tx < tiles[0]; tx++) {
+        const float lo_off = p->band + 1.0f, hi_off = (3.0f + p->band) + 1.0f;
+        const v3 tl = V((float)(tx * 4) - lo_off, (float)(ty * 4) - lo_off, (float)(tz * 4) - lo_off);
+        const v3 th = V((float)(tx * 4) + hi_off, (float)(ty * 4) + hi_off, (float)(tz * 4) + hi_off);
+        int nc = 0;   /* candidates in index order, at most MAXC (coupling.js:100-124) */
+        for (int32_t bi = 0; bi < n && nc < SIO_MAXC; bi++) {
+          const float* b = bodies + 48 * (size_t)bi;
+          if ((f2u(b[46]) & (SIO_F_DISABLED | SIO_F_SENSOR)) != 0u || (f2u(b[44]) & p->mask) == 0u) continue;
+          const v3 c = vscale(p->inv_dx, vsub(vadd(V(b[0], b[1], b[2]), vscale(p->lead, V(b[8], b[9], b[10]))), origin));
+          const v3 q = V(clampf(c.x, tl.x, th.x), clampf(c.y, tl.y, th.y), clampf(c.z, tl.z, th.z));
+          if (vlen(vsub(c, q)) <= b[3] * p->inv_dx) cand[nc++] = bi;
+        }
+        if (nc == 0) continue;
+        memset(accj, 0, sizeof(int32_t) * 3 * (size_t)nc);
+        memset(accl, 0, sizeof(int32_t) * 3 * (size_t)nc);
+        for (int lz = 0; lz < 4; lz++)
+          for (int ly = 0; ly < 4; ly++)
+            for (int lx = 0; lx < 4; lx++) {
+              const int32_t gx = tx * 4 + lx, gy = ty * 4 + ly, gz = tz * 4 + lz;
+              if (gx >= dims[0] || gy >= dims[1] || gz >= dims[2]) continue;
+              int32_t* node = grid + 4 * ((size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz));
+              const float m = i2f_bits(node[3]);
+              if (!(m > 0.0f)) continue;
+              v3 v = V(i2f_bits(node[0]), i2f_bits(node[1]), i2f_bits(node[2]));
+              const v3 pw = vadd(origin, vscale(p->dx, V((float)gx, (float)gy, (float)gz)));
+              for (int c = 0; c < nc; c++) {
+                const float* b = bodies + 48 * (size_t)cand[c];
+                const v3 bc = vadd(V(b[0], b[1], b[2]), vscale(p->lead, V(b[8], b[9], b[10])));
+                float dist;
+                v3 nr;
+                body_sdf(b, bc, pw, &dist, &nr);
+                if (!(dist * p->inv_dx < p->band)) continue;
+                const v3 r = vsub(pw, bc);
+                const v3 vb = vscale(p->vel_to_lattice, vadd(V(b[8], b[9], b[10]), vcross(V(b[12], b[13], b[14]), r)));
+                v3 vr = vsub(v, vb);
+                const float vn = vdot(vr, nr);
+                if (vn < 0.0f) {
+                  vr = vsub(vr, vscale(vn, nr));
+                  const float vt = vlen(vr);
+                  if (vt > 1e-9f) vr = vscale(fmaxf(0.0f, 1.0f - (p->friction * -vn) / vt), vr);
+                  const v3 vnew = vadd(vr, vb);
+                  if (b[36] > 0.0f) {
+                    const v3 J = vscale(-m, vsub(vnew, v));
+                    const v3 L = vcross(vscale(p->inv_dx, r), J);
+                    accj[c * 3] += wgsl_i32(rintf(J.x * SIO_FPJ));
+                    accj[c * 3 + 1] += wgsl_i32(rintf(J.y * SIO_FPJ));
+                    accj[c * 3 + 2] += wgsl_i32(rintf(J.z * SIO_FPJ));
+                    accl[c * 3] += wgsl_i32(rintf(L.x * SIO_FPL));
+                    accl[c * 3 + 1] += wgsl_i32(rintf(L.y * SIO_FPL));
+                    accl[c * 3 + 2] += wgsl_i32(rintf(L.z * SIO_FPL));
+                  }
+                  v = vnew;
+                }
+              }
+              node[0] = f2i_bits(v.x); node[1] = f2i_bits(v.y); node[2] = f2i_bits(v.z); node[3] = f2i_bits(m);
+            }
+        for (int k = 0; k < nc * 3; k++) {
+          const int32_t bi = cand[k / 3], a = k % 3;
+          acc[bi * 8 + a] = (int32_t)((uint32_t)acc[bi * 8 + a] + (uint32_t)accj[k]);
+          acc[bi * 8 + 4 + a] = (int32_t)((uint32_t)acc[bi * 8 + 4 + a] + (uint32_t)accl[k]);
+        }
+      }
+}
+
+void sio_couple_apply(int32_t* acc, float* ext, int32_t n, float mom_to_world, float dx) {
+  for (int32_t i = 0; i < n; i++) {
+    int32_t* a = acc + 8 * (size_t)i;
+    if (a[0] == 0 && a[1] == 0 && a[2] == 0 && a[4] == 0 && a[5] == 0 && a[6] == 0) continue;
+    for (int k = 0; k < 3; k++) {
+      ext[8 * i + k] = ext[8 * i + k] + ((float)a[k] / SIO_FPJ) * mom_to_world;
+      ext[8 * i + 4 + k] = ext[8 * i + 4 + k] + (((float)a[4 + k] / SIO_FPL) * mom_to_world) * dx;
+    }
+    memset(a, 0, 8 * sizeof(int32_t));
+  }
+}
+
 /* ------------------------------------------------------------------ emission, mpm.js:683-714 + 213-227 */
 static inline double js_maxd(double a, double b) { return (a != a || b != b) ? (double)NAN : (a > b ? a : b); }
 static inline double js_mind(double a, double b) { return (a != a || b != b) ? (double)NAN : (a < b ? a : b); }
@@ -590,6 +739,11 @@ void sio_substeps(float* P, float* scratch, int64_t n, int32_t* grid, const sio_
     }
     sio_p2g(cur, n, prm->dims, prm->mats, prm->vol4, grid, threads);
     sio_grid_update(grid, prm->dims, prm->gravity, prm->bound, prm->cols, prm->ncol, prm->floor_friction, threads);
+    if (prm->nbodies > 0) {   /* coupling.substep(s), mpm.js:596 */
+      sio_couple_params cp = prm->couple;
+      cp.lead = (float)(((double)s + 0.5) * prm->substep_dt);
+      sio_couple(grid, prm->dims, prm->bodies, prm->nbodies, &cp, prm->body_acc);
+    }
     sio_g2p(cur, n, prm->dims, grid, prm->mats, prm->bound, prm->vmax, threads);
     (*step_count)++;
   }

@@ -14,6 +14,7 @@
  *   G2P + fluid / Neo-Hookean / snow / sand ......... mpm.js:474-560
  *   eigSym3 / svd3 (4 cyclic Jacobi sweeps) .......... src/shaders/linalg.js:14-69
  *   step() schedule ................................. mpm.js:582-604
+ *   fluid <-> rigid coupling pass and apply ......... src/physics/coupling.js:31-60, 83-196
  *
  * Canonical f32 evaluation order. WGSL pins neither FMA contraction nor the reduction order of
  * matrix products, so this file fixes one order and the CUDA kernels follow it exactly:
@@ -70,6 +71,15 @@ void sio_g2p(float* P, int64_t n, const int32_t dims[3], const int32_t* grid, co
              float bound, float vmax, int threads);
 void sio_retime(float* P, int64_t n, float k);
 
+typedef struct {
+  float origin[3];        /* world origin of node 0 */
+  float dx, inv_dx;
+  float lead;             /* body positions extrapolated by v * lead: (s + 0.5) * substep dt */
+  float vel_to_lattice;   /* substep dt / dx */
+  float friction, band;   /* fluid-body friction (0.2), band in cells (0.5) */
+  uint32_t mask;          /* group bits of the bodies that interact */
+} sio_couple_params;
+
 typedef struct sio_params {
   int32_t dims[3];
   uint32_t num_blocks;
@@ -82,6 +92,13 @@ typedef struct sio_params {
   int32_t ncol;
   const float* mats;    /* 8 x 12 */
   const float* cols;    /* 16 x 12 */
+  /* rigid coupling (nbodies = 0: none): body records, pass parameters (lead is set per substep
+   * as (s + 0.5) * substep_dt, s counted from the call's first substep), impulse sums */
+  const float* bodies;
+  int32_t nbodies;
+  sio_couple_params couple;
+  double substep_dt;
+  int32_t* body_acc;
 } sio_params;
 
 /* K substeps of mpm.js:590-602 starting at *step_count. P holds the n records on entry and on
@@ -99,6 +116,20 @@ float sio_logf(float x);
 float sio_expf(float x);
 /* svd3 of linalg.js:46-69 on a column-major 3x3 (m[col*3+row]); outputs U, s, V likewise. */
 void sio_svd3(const float* F, float* U, float* s, float* V);
+
+/* ---- fluid <-> rigid coupling, src/physics/coupling.js:83-196 (moving rigid boundaries of the grid)
+ * bodies: n records of 48 floats, the reference's Body (src/physics/rigid-wgsl.js:20-33): x (w =
+ * bounding radius), q (x y z w), v (w = friction), w (angular velocity), x0, q0, y, qy, size (w =
+ * shape: 0 sphere, 1 box, 2 capsule), mass (x = m, 0 = static / kinematic), props, info (4 u32:
+ * group bits, mask bits, flags, user). sio_couple runs the pass of one substep over a grid that
+ * holds vec4f(v, m) bits (after the grid update): nodes with m > 0 within `band` cells of a body
+ * lose their inward relative velocity (Coulomb friction on the tangent), and the reaction impulses
+ * are added in fixed point to acc (n x 8 i32: J x 16384 in [0..2], L x 1024 in [4..6]). */
+
+void sio_couple(int32_t* grid, const int32_t dims[3], const float* bodies, int32_t n,
+                const sio_couple_params* p, int32_t* acc);
+/* mpm-rigid-apply: ext (n x 8 f32: J xyz 0, L xyz 0) += acc in world units, acc zeroed. */
+void sio_couple_apply(int32_t* acc, float* ext, int32_t n, float mom_to_world, float dx);
 
 #ifdef __cplusplus
 }

@@ -16,11 +16,18 @@ u32_p = ctypes.POINTER(ctypes.c_uint32)
 i64_p = ctypes.POINTER(ctypes.c_int64)
 
 
+class CoupleParams(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("dx", ctypes.c_float), ("inv_dx", ctypes.c_float),
+                ("lead", ctypes.c_float), ("vel_to_lattice", ctypes.c_float), ("friction", ctypes.c_float),
+                ("band", ctypes.c_float), ("mask", ctypes.c_uint32)]
+
+
 class Params(ctypes.Structure):
     _fields_ = [("dims", ctypes.c_int32 * 3), ("num_blocks", ctypes.c_uint32), ("gravity", ctypes.c_float * 3),
                 ("bound", ctypes.c_float), ("floor_friction", ctypes.c_float), ("vmax", ctypes.c_float),
                 ("vol4", ctypes.c_float), ("sort_every", ctypes.c_int32), ("ncol", ctypes.c_int32),
-                ("mats", f_p), ("cols", f_p)]
+                ("mats", f_p), ("cols", f_p), ("bodies", f_p), ("nbodies", ctypes.c_int32),
+                ("couple", CoupleParams), ("substep_dt", ctypes.c_double), ("body_acc", i32_p)]
 
 
 def lib():
@@ -49,6 +56,8 @@ def lib():
         L.sio_expf.restype = ctypes.c_float
         L.sio_expf.argtypes = [ctypes.c_float]
         L.sio_svd3.argtypes = [f_p, f_p, f_p, f_p]
+        L.sio_couple.argtypes = [i32_p, i32_p, f_p, ctypes.c_int32, ctypes.POINTER(CoupleParams), i32_p]
+        L.sio_couple_apply.argtypes = [i32_p, f_p, ctypes.c_int32, ctypes.c_float, ctypes.c_float]
         d3 = ctypes.POINTER(ctypes.c_double)
         L.sio_emit_box.restype = ctypes.c_int64
         L.sio_emit_box.argtypes = [d3, d3, ctypes.c_double, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32, d3,
@@ -135,7 +144,7 @@ def retime(P, k):
 
 
 def substeps(P, dims, mats, cols, ncol, gravity, vol4, K, step_count=0, sort_every=4, threads=1,
-             bound=3.0, floor_friction=0.4, vmax=0.9):
+             bound=3.0, floor_friction=0.4, vmax=0.9, coupling=None):
     """K substeps of mpm.js:590-602 on records P; returns (P, grid i32 words, step_count)."""
     P = np.array(P, np.float32, copy=True)
     scratch = np.empty_like(P)
@@ -150,6 +159,42 @@ def substeps(P, dims, mats, cols, ncol, gravity, vol4, K, step_count=0, sort_eve
     prm.bound, prm.floor_friction, prm.vmax, prm.vol4 = bound, floor_friction, vmax, vol4
     prm.sort_every, prm.ncol = sort_every, ncol
     prm.mats, prm.cols = _f(mats), _f(cols)
+    keep = []
+    if coupling is not None:   # dict(bodies, params (9 floats: origin xyz dx inv_dx - vel friction band), mask, dt, acc)
+        b = np.ascontiguousarray(coupling["bodies"], np.float32).reshape(-1, 48)
+        acc = coupling["acc"]
+        keep += [b, acc]
+        prm.bodies, prm.nbodies, prm.body_acc = _f(b), len(b), _i(acc)
+        q = coupling["params"]
+        for k in range(3):
+            prm.couple.origin[k] = float(q[k])
+        prm.couple.dx, prm.couple.inv_dx, _, prm.couple.vel_to_lattice, prm.couple.friction, prm.couple.band = \
+            [float(x) for x in q[3:9]]
+        prm.couple.mask = int(coupling["mask"])
+        prm.substep_dt = float(coupling["dt"])
     sc = ctypes.c_int64(step_count)
     lib().sio_substeps(_f(P), _f(scratch), len(P), _i(grid), ctypes.byref(prm), ctypes.byref(sc), K, threads)
     return P, grid, sc.value
+
+
+def couple(grid, dims, bodies, params, mask):
+    """The coupling pass of one substep (coupling.js:83-186) on a grid of vec4f(v, m) bits.
+    params: origin xyz, dx, inv_dx, lead, vel_to_lattice, friction, band. Returns (grid, acc)."""
+    g = np.array(grid, np.int32, copy=True)
+    b = np.ascontiguousarray(bodies, np.float32).reshape(-1, 48)
+    acc = np.zeros(len(b) * 8, np.int32)
+    cp = CoupleParams()
+    for k in range(3):
+        cp.origin[k] = float(params[k])
+    cp.dx, cp.inv_dx, cp.lead, cp.vel_to_lattice, cp.friction, cp.band = [float(x) for x in params[3:9]]
+    cp.mask = int(mask)
+    lib().sio_couple(_i(g), _i(dims_arr(dims)), _f(b), len(b), ctypes.byref(cp), _i(acc))
+    return g, acc
+
+
+def couple_apply(acc, n, mom_to_world, dx):
+    """mpm-rigid-apply (coupling.js:188-196): world impulses (n x 8) from the fixed-point sums."""
+    a = np.array(acc, np.int32, copy=True)
+    ext = np.zeros(n * 8, np.float32)
+    lib().sio_couple_apply(_i(a), _f(ext), n, mom_to_world, dx)
+    return ext.reshape(n, 8), a

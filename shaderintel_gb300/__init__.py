@@ -4,7 +4,7 @@ The CUDA library (libsi_cuda, C ABI in include/si_cuda.h) holds the kernels and 
 package is the host side over it, mirroring the reference's JavaScript MPM object.
 """
 from ._lib import SIError, lib
-from .mpm import FLUID, JELLY, MATERIALS, MPM, MPM_KINDS, SAND, SNOW, World, material_row, sample_shape
+from .mpm import FLUID, JELLY, MATERIALS, MPM, MPM_KINDS, SAND, SNOW, World, body_record, material_row, sample_shape
 
 __all__ = ["MPM", "World", "SIError", "MATERIALS", "MPM_KINDS", "FLUID", "JELLY", "SNOW", "SAND", "lib",
-           "material_row", "sample_shape"]
+           "material_row", "sample_shape", "body_record"]

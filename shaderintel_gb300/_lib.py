@@ -95,6 +95,10 @@ SIGNATURES = {
                                        c_float_p]),
     "si_collider_row": (ctypes.c_int, [vp, ctypes.c_int32, c_double_p, c_double_p, ctypes.c_double, ctypes.c_double,
                                        c_double_p, ctypes.c_double, c_float_p]),
+    "si_mpm_couple": (ctypes.c_int, [vp, c_float_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_uint32,
+                                     ctypes.c_double]),
+    "si_mpm_set_bodies": (ctypes.c_int, [vp, c_float_p, ctypes.c_int32]),
+    "si_mpm_read_impulses": (ctypes.c_int, [vp, c_float_p, ctypes.c_int32]),
     "si_server_create": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.POINTER(vp)]),
     "si_server_destroy": (ctypes.c_int, [vp]),
     "si_server_admit": (ctypes.c_int, [vp, ctypes.POINTER(si_mpm_desc), ctypes.POINTER(vp)]),

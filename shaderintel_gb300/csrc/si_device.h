@@ -34,7 +34,8 @@ constexpr uint32_t F_FORCE_GLOBAL = 16u; // P2G skips the shared-memory tile (mp
 constexpr uint32_t F_NO_CLEAR_NEXT = 32u; // grid update leaves grid_next alone
 constexpr uint32_t F_KEYS_NOW = 64u;  // compute the block keys of the current positions before the sort
 constexpr uint32_t F_CLEAR = 128u;    // zero `grid` before the standalone P2G
-constexpr uint32_t F_BOXED = 256u;    // grid update: nodes outside box_cur + box_next are zero in both arrays
+constexpr uint32_t F_BOXED = 256u;
+constexpr uint32_t F_COUPLE = 512u;   // run the fluid <-> rigid coupling pass after the grid update    // grid update: nodes outside box_cur + box_next are zero in both arrays
 
 struct SceneParams {             // per scene, device resident, rewritten when a value changes
   float4 mats[24];               // 8 materials x 3 vec4 (mpm.js:116)
@@ -47,6 +48,15 @@ struct SceneParams {             // per scene, device resident, rewritten when a
   float vmax;                    // 0.9
   float vol4;                    // 4 / ppcAxis^3
   uint32_t num_blocks;
+  // fluid <-> rigid coupling (src/physics/coupling.js): body table and pass parameters
+  const float4* bodies;          // nbodies x 12 float4, the reference's Body record
+  int32_t* body_acc;             // nbodies x 8 i32: J x 16384 [0..2], L x 1024 [4..6]
+  int32_t nbodies;
+  uint32_t body_mask;            // group bits of the bodies that interact
+  float origin[3];               // world origin of node 0
+  float dx, inv_dx;
+  float vel_to_lattice;          // substep dt / dx
+  float friction, band;          // 0.2, 0.5 cells
 };
 
 struct TickScene {               // per tick and active scene, host built
@@ -66,6 +76,8 @@ struct TickScene {               // per tick and active scene, host built
   uint32_t bin_base;             // first global bin of this scene
   uint32_t pchunk_begin;         // first particle chunk of this scene (prefix over the tick)
   uint32_t nchunk_begin;         // first node chunk
+  uint32_t cchunk_begin;         // first 4^3 node tile of the coupling pass
+  float lead;                    // coupling: bodies extrapolated by v * lead = (s + 0.5) * dt
 };
 
 struct TickInfo {                // one tick's totals (kernel arguments)
@@ -75,6 +87,7 @@ struct TickInfo {                // one tick's totals (kernel arguments)
   uint32_t nchunks;              // node chunks
   int32_t chunk;                 // particles per chunk (= kCtaThreads * ppt)
   int32_t tile_nodes;            // shared tile capacity in nodes
+  uint32_t cchunks;              // 4^3 node tiles of the coupled scenes
 };
 
 struct SortInfo {                // one tick's sort
@@ -92,6 +105,7 @@ void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_clear(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_box_reset(const TickInfo& t, cudaStream_t st);
+void launch_couple(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
 void launch_reorder(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
 void launch_keys(const TickInfo& t, int grid_ctas, cudaStream_t st);

@@ -158,6 +158,17 @@ static void build_params(const si_mpm* h, SceneParams* p) {
   p->vmax = 0.9f;             // mpm.js:599
   p->vol4 = (float)(4 * (1.0 / std::pow((double)h->ppc_axis, 3.0)));   // mpm.js:589,610
   p->num_blocks = h->num_blocks;
+  // coupling uniforms, coupling.js:212-214 (JavaScript numbers written as f32)
+  p->bodies = h->bodies;
+  p->body_acc = h->body_acc;
+  p->nbodies = h->nbodies;
+  p->body_mask = h->body_mask;
+  for (int a = 0; a < 3; a++) p->origin[a] = (float)h->origin[a];
+  p->dx = (float)h->dx;
+  p->inv_dx = (float)(1.0 / h->dx);
+  p->vel_to_lattice = (float)(h->dt / h->dx);
+  p->friction = (float)h->friction;
+  p->band = (float)h->band;
 }
 
 static int upload_params(si_mpm* h) {
@@ -182,8 +193,8 @@ enum TickMode { T_SUBSTEP = 0, T_P2G = 1, T_GRID = 2, T_G2P = 3, T_SORT = 4 };
 struct HostTick {
   int mode = T_SUBSTEP;
   std::vector<TickScene> ts;
-  std::vector<uint32_t> nb, nck;     // per entry: num_blocks, node chunks (host side only)
-  uint32_t pchunks = 0, nchunks = 0;
+  std::vector<uint32_t> nb, nck, nct;   // per entry: num_blocks, node chunks, coupling tiles (host side)
+  uint32_t pchunks = 0, nchunks = 0, cchunks = 0;
   bool any_p2g = false, any_clear = false, any_gather = false, any_keys_now = false;
   uint32_t sort_n = 0, sort_bins = 0, max_blocks = 0;
   int passes = 0;
@@ -203,12 +214,14 @@ static TickScene base_entry(si_mpm* h) {
 }
 
 static void finish_tick(si_world* w, HostTick& k) {
-  uint32_t pc = 0, nc = 0, seg = 0, bin = 0;
+  uint32_t pc = 0, nc = 0, cc = 0, seg = 0, bin = 0;
   const uint32_t chunk = (uint32_t)(kCtaThreads * w->ppt);
   for (size_t e = 0; e < k.ts.size(); e++) {
     TickScene& t = k.ts[e];
     t.pchunk_begin = pc;
     t.nchunk_begin = nc;
+    t.cchunk_begin = cc;
+    cc += k.nct[e];
     pc += (uint32_t)((t.n + chunk - 1) / chunk);
     if (t.flags & F_P2G) k.any_p2g = true;
     if (t.flags & F_CLEAR) k.any_clear = true;
@@ -225,6 +238,7 @@ static void finish_tick(si_world* w, HostTick& k) {
   }
   k.pchunks = pc;
   k.nchunks = nc;
+  k.cchunks = cc;
   k.sort_n = seg;
   k.sort_bins = bin;
   int bits = 1;
@@ -236,6 +250,7 @@ static void push_entry(HostTick& k, const si_mpm* h, const TickScene& t) {
   k.ts.push_back(t);
   k.nb.push_back(h->num_blocks);
   k.nck.push_back((uint32_t)((h->nodes + kNodeChunk - 1) / kNodeChunk));
+  k.nct.push_back((t.flags & F_COUPLE) ? (uint32_t)(((h->dims[0] + 3) / 4) * ((h->dims[1] + 3) / 4) * ((h->dims[2] + 3) / 4)) : 0u);
 }
 
 static TickScene substep_entry(si_mpm* h) {
@@ -255,6 +270,11 @@ static TickScene substep_entry(si_mpm* h) {
   // `grid` (the previous G2P, or the standalone P2G of a substep that started after box_ok was
   // reset), box_next from the one before, whose grid update left values only inside it
   if (h->box_ok >= 2) f |= F_BOXED;
+  if (h->nbodies > 0) {   // coupling.substep(s) after the grid update, mpm.js:596; lead = (s + 0.5) dt
+    f |= F_COUPLE;
+    t.lead = (float)((h->frame_sub + 0.5) * h->dt);
+  }
+  h->frame_sub++;
   t.flags = f;
   // state after the substep
   h->gcur = 1 - h->gcur;
@@ -301,6 +321,7 @@ static int64_t tick_kernels(const HostTick& k) {
   if (k.any_p2g) n++;
   if (k.mode == T_SUBSTEP || k.mode == T_GRID) n++;
   if (k.mode == T_SUBSTEP) n++;   // box reset
+  if (k.cchunks) n++;
   if (k.mode == T_SUBSTEP || k.mode == T_G2P) n++;
   return n;
 }
@@ -311,6 +332,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   t.nscenes = (int32_t)k.ts.size();
   t.pchunks = k.pchunks;
   t.nchunks = k.nchunks;
+  t.cchunks = k.cchunks;
   t.chunk = kCtaThreads * w->ppt;
   t.tile_nodes = w->tile_nodes;
   cudaStream_t st = w->st;
@@ -332,6 +354,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   if (k.any_p2g) launch_p2g(t, w->ctas_p2g, st);
   if (profile) cudaEventRecord(w->pev[2], st);
   if (k.mode == T_SUBSTEP || k.mode == T_GRID) launch_grid(t, w->ctas_grid, st);
+  if (k.cchunks) launch_couple(t, w->sms * 16, st);
   if (k.mode == T_SUBSTEP) launch_box_reset(t, st);   // box_next starts empty for the fused P2G
   if (profile) cudaEventRecord(w->pev[3], st);
   if (k.mode == T_SUBSTEP || k.mode == T_G2P) launch_g2p(t, perm, w->ctas_g2p, st);
@@ -359,7 +382,7 @@ static bool same_plan(const GraphPlan& g, const std::vector<HostTick>& plan, con
   for (size_t i = 0; i < plan.size(); i++) {
     const HostTick& a = plan[i];
     const GraphTick& b = g.ticks[i];
-    if (a.mode != b.mode || a.pchunks != b.pchunks || a.nchunks != b.nchunks || a.any_p2g != b.any_p2g ||
+    if (a.mode != b.mode || a.pchunks != b.pchunks || a.nchunks != b.nchunks || a.cchunks != b.cchunks || a.any_p2g != b.any_p2g ||
         a.any_clear != b.any_clear || a.any_gather != b.any_gather || a.any_keys_now != b.any_keys_now ||
         a.sort_n != b.sort_n || a.passes != b.passes)
       return false;
@@ -425,7 +448,7 @@ static int run_plan(si_world* w, std::vector<HostTick>& plan) {
     g->tile_nodes = w->tile_nodes;
     for (const HostTick& k : plan) {
       GraphTick t;
-      t.mode = k.mode; t.pchunks = k.pchunks; t.nchunks = k.nchunks; t.any_p2g = k.any_p2g;
+      t.mode = k.mode; t.pchunks = k.pchunks; t.nchunks = k.nchunks; t.cchunks = k.cchunks; t.any_p2g = k.any_p2g;
       t.any_clear = k.any_clear; t.any_gather = k.any_gather; t.any_keys_now = k.any_keys_now;
       t.sort_n = k.sort_n; t.passes = k.passes;
       g->ticks.push_back(t);
@@ -555,8 +578,11 @@ static void scene_release(si_mpm* h) {
   si_world* w = h->w;
   h->destroyed = true;
   for (void* p : {(void*)h->pbuf[0], (void*)h->pbuf[1], (void*)h->grid[0], (void*)h->grid[1], (void*)h->keys,
-                  (void*)h->starts, (void*)h->prm, (void*)h->box})
+                  (void*)h->starts, (void*)h->prm, (void*)h->box, (void*)h->bodies, (void*)h->body_acc})
     if (p) cudaFreeAsync(p, w->st);
+  h->bodies = nullptr;
+  h->body_acc = nullptr;
+  h->nbodies = 0;
   h->pbuf[0] = h->pbuf[1] = nullptr;
   h->grid[0] = h->grid[1] = nullptr;
   h->keys = h->starts = nullptr;
@@ -588,6 +614,7 @@ int si_world_destroy(si_world* w) {
 int si_world_step(si_world* w, int32_t K) {
   GUARD_WORLD(w);
   if (K <= 0) return si_fail(SI_EINVAL, "si_world_step: K must be > 0");
+  for (si_mpm* h : w->scenes) h->frame_sub = 0;
   return run_substeps(w, w->scenes, K);
 }
 
@@ -895,6 +922,64 @@ int si_mpm_set_colliders(si_mpm* h, const float* rows, int32_t k) {
   return SI_OK;
 }
 
+int si_mpm_couple(si_mpm* h, const float* bodies, int32_t n, double friction, double band, uint32_t mask,
+                  double density_scale) {
+  GUARD(h);
+  if (n < 0 || (n && !bodies)) return si_fail(SI_EINVAL, "MPM.couple: bad body table");
+  cudaStream_t st = h->w->st;
+  if (h->bodies) CK(cudaFreeAsync(h->bodies, st));
+  if (h->body_acc) CK(cudaFreeAsync(h->body_acc, st));
+  h->bodies = nullptr;
+  h->body_acc = nullptr;
+  h->nbodies = 0;
+  h->prm_dirty = true;
+  if (n == 0) return SI_OK;   // uncouple(), mpm.js:255-259
+  CK(cudaMallocAsync((void**)&h->bodies, (size_t)n * 192, st));
+  CK(cudaMallocAsync((void**)&h->body_acc, (size_t)n * 32, st));
+  CK(cudaMemcpyAsync(h->bodies, bodies, (size_t)n * 192, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(h->body_acc, 0, (size_t)n * 32, st));
+  CK(cudaStreamSynchronize(st));   // the host table may be reused by the caller
+  h->nbodies = n;
+  h->friction = friction;
+  h->band = band;
+  h->body_mask = mask;
+  h->density_scale = density_scale;
+  return SI_OK;
+}
+
+int si_mpm_set_bodies(si_mpm* h, const float* bodies, int32_t n) {
+  GUARD(h);
+  if (!bodies || n != h->nbodies) return si_fail(SI_EINVAL, "MPM: the body table must keep the coupled count");
+  if (n == 0) return SI_OK;
+  CK(cudaMemcpyAsync(h->bodies, bodies, (size_t)n * 192, cudaMemcpyHostToDevice, h->w->st));
+  CK(cudaStreamSynchronize(h->w->st));
+  return SI_OK;
+}
+
+int si_mpm_read_impulses(si_mpm* h, float* out, int32_t n) {
+  GUARD(h);
+  if (!out || n != h->nbodies) return si_fail(SI_EINVAL, "MPM: impulses are read for the coupled bodies");
+  if (n == 0) return SI_OK;
+  std::vector<int32_t> acc((size_t)n * 8);
+  CK(cudaMemcpyAsync(acc.data(), h->body_acc, (size_t)n * 32, cudaMemcpyDeviceToHost, h->w->st));
+  CK(cudaMemsetAsync(h->body_acc, 0, (size_t)n * 32, h->w->st));
+  CK(cudaStreamSynchronize(h->w->st));
+  // mpm-rigid-apply, coupling.js:188-196, on the host: momToWorld = densityScale dx^4 / dt (f32)
+  const float m2w = (float)(h->density_scale * std::pow(h->dx, 4.0) / h->dt);
+  const float dx = (float)h->dx;
+  for (int32_t i = 0; i < n; i++) {
+    const int32_t* a = acc.data() + 8 * (size_t)i;
+    float* o = out + 8 * (size_t)i;
+    std::memset(o, 0, 8 * sizeof(float));
+    if (a[0] == 0 && a[1] == 0 && a[2] == 0 && a[4] == 0 && a[5] == 0 && a[6] == 0) continue;
+    for (int k = 0; k < 3; k++) {
+      o[k] = 0.0f + ((float)a[k] / 16384.0f) * m2w;
+      o[4 + k] = 0.0f + (((float)a[4 + k] / 1024.0f) * m2w) * dx;
+    }
+  }
+  return SI_OK;
+}
+
 int si_mpm_set_gravity(si_mpm* h, const double g[3]) {
   GUARD(h);
   if (!g) return si_fail(SI_EINVAL, "null gravity");
@@ -938,6 +1023,7 @@ int si_mpm_step(si_mpm* h, double dt, int32_t K) {
   }
   if (K <= 0) K = h->substeps;
   if (h->count == 0) return SI_OK;   // mpm.js:584
+  h->frame_sub = 0;
   std::vector<si_mpm*> one{h};
   return run_substeps(h->w, one, K);
 }

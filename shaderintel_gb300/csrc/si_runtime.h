@@ -13,7 +13,7 @@
 
 struct GraphTick {
   int mode;
-  uint32_t pchunks, nchunks;
+  uint32_t pchunks, nchunks, cchunks;
   bool any_p2g, any_clear, any_gather, any_keys_now;
   uint32_t sort_n;
   int passes;
@@ -92,6 +92,13 @@ struct si_mpm {
   uint32_t* starts = nullptr;
   int32_t* box = nullptr;           // [2][8]: stencil-base box of the P2G that filled grid[0] / grid[1]
   int box_ok = 0;                   // standard substeps in a row (>= 2: both boxes describe the arrays)
+  // fluid <-> rigid coupling (src/physics/coupling.js): the body table and its impulse sums
+  float4* bodies = nullptr;         // nbodies x 12 float4
+  int32_t* body_acc = nullptr;      // nbodies x 8 i32
+  int32_t nbodies = 0;
+  uint32_t body_mask = 0xffffffffu;
+  double friction = 0.2, band = 0.5, density_scale = 1.0;
+  int32_t frame_sub = 0;            // substeps since the step call began (the coupling's lead)
   si::SceneParams* prm = nullptr;
   bool prm_dirty = true;
   bool pending = false;             // grid[1-gcur] holds the P2G of the current particle state

@@ -118,6 +118,7 @@ static void server_loop(si_server* s) {
     auto* comp = new Completion{s, {}, 0, (int64_t)K};
     for (si_mpm* h : act) {
       Request* r = s->queues[h].front();
+      if (r->remaining == r->K) h->frame_sub = 0;   // a request is one step(dt, K) call
       r->remaining -= K;
       fin.push_back(nullptr);
       if (r->remaining <= 0) {

@@ -91,6 +91,30 @@ def sample_shape(shape, spacing, jitter, seed):
     return out
 
 
+SHAPES = {"sphere": 0, "box": 1, "capsule": 2}   # src/physics/rigid-wgsl.js:12
+
+
+def body_record(position, size, shape="sphere", quaternion=(0, 0, 0, 1), velocity=(0, 0, 0),
+                angular_velocity=(0, 0, 0), mass=0.0, friction=0.5, group=1, mask=0xFFFFFFFF, flags=0, radius=None):
+    """One Body record of src/physics/rigid-wgsl.js:20-33 (48 floats, world units) for MPM.couple:
+    size = sphere (r, r, r), box half extents, capsule (r, half length, r); mass 0 = static;
+    radius = bounding radius (default from the shape)."""
+    r = np.zeros(48, np.float32)
+    sz = np.asarray(size, np.float64)
+    k = SHAPES[shape] if isinstance(shape, str) else int(shape)
+    if radius is None:
+        radius = float(sz[0]) if k == 0 else (float(np.linalg.norm(sz)) if k == 1 else float(sz[0] + sz[1]))
+    q = np.asarray(quaternion, np.float64)
+    r[0:3], r[3] = position, radius
+    r[4:8] = q / np.linalg.norm(q)
+    r[8:11], r[11] = velocity, friction
+    r[12:15] = angular_velocity
+    r[32:35], r[35] = sz, k
+    r[36] = mass
+    r[44:48] = np.array([group, mask, flags, 0], np.uint64).astype(np.uint32).view(np.float32)
+    return r
+
+
 class World:
     """A CUDA stream and the simulations stepped together on it (the batched form)."""
 
@@ -346,6 +370,32 @@ class MPM:
         d = float(dt) if dt else 0.0
         self._upload_colliders(d)
         check(L.lib().si_mpm_step(self._h, d, int(K or 0)))
+
+    # ---------------------------------------------------------------- rigid coupling (mpm.js:244-259)
+    def couple(self, bodies, friction=0.2, band=0.5, mask=0xFFFFFFFF, densityScale=1.0):
+        """Two-way coupling with rigid bodies (src/physics/coupling.js): `bodies` is an (n, 48)
+        float32 array of the reference's Body records (see body_record). Empty uncouples."""
+        b = np.ascontiguousarray(bodies, np.float32).reshape(-1, 48)
+        check(L.lib().si_mpm_couple(self._h, fptr(b) if len(b) else None, len(b), float(friction), float(band),
+                                    int(mask) & 0xFFFFFFFF, float(densityScale)))
+        self._nbodies = len(b)
+
+    def uncouple(self):
+        self.couple(np.zeros((0, 48), np.float32))
+
+    def setBodies(self, bodies):
+        """New poses and velocities of the coupled bodies (the rigid world stepped)."""
+        b = np.ascontiguousarray(bodies, np.float32).reshape(-1, 48)
+        check(L.lib().si_mpm_set_bodies(self._h, fptr(b), len(b)))
+
+    def readImpulses(self):
+        """The bodies' reaction impulses since the last read, world units: (n, 8) float32 with
+        J in [:, 0:3] and L in [:, 4:7] (coupling.finish(), mpm-rigid-apply)."""
+        n = getattr(self, "_nbodies", 0)
+        out = np.zeros((n, 8), np.float32)
+        if n:
+            check(L.lib().si_mpm_read_impulses(self._h, fptr(out), n))
+        return out
 
     def p2g(self, forceGlobal=False):
         """Clear the grid and scatter the particles (forceGlobal: skip the shared-memory tile)."""

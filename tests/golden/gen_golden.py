@@ -222,5 +222,98 @@ def main(ref):
     print("trajectory", rec4.shape, K)
 
 
+
+
+
+# ============================================================================ fluid <-> rigid coupling
+BODY_FIELDS = ["x", "q", "v", "w", "x0", "q0", "y", "qy", "size", "mass", "props", "info"]
+
+
+def coupling_sources(ref):
+    """The coupling module and kernels of src/physics/coupling.js with the parts of the rigid and
+    math modules they use (Body, its flags and shapeOf from src/physics/rigid-wgsl.js:20-37,75;
+    qmat from src/shaders/math.js:56-62)."""
+    cpl = open(os.path.join(ref, "src/physics/coupling.js")).read()
+    rig = open(os.path.join(ref, "src/physics/rigid-wgsl.js")).read()
+    mth = open(os.path.join(ref, "src/shaders/math.js")).read()
+    a = rig.index("struct Body {")
+    body = rig[a:rig.index("}", a) + 1]
+    flags = "\n".join(l for l in rig.splitlines() if l.startswith("const F_"))
+    a = rig.index("fn shapeOf(")
+    shape = rig[a:rig.index("\n", a)]
+    a = mth.index("fn qmat(")
+    qmat = mth[a:mth.index("\n}\n", a) + 2]
+    mods = "\n".join([body, flags, shape, qmat, W.field_template(cpl, "defineModule('coupling'", "code")])
+    vals = {"MAX_CAND": "128", "MAX_CAND * 3": "384", "FPJ": "16384", "FPL": "1024"}
+    couple = (W.substitute(W.field_template(cpl, "name: 'mpm-rigid-couple'", "shared"), vals),
+              W.substitute(W.field_template(cpl, "name: 'mpm-rigid-couple'", "code"), vals))
+    apply = W.substitute(W.field_template(cpl, "name: 'mpm-rigid-apply'", "code"), vals)
+    return mods, couple, apply
+
+
+def body_record(pos, quat, vel, angvel, shape, size, mass, radius, group=1, mask=0xFFFFFFFF, flags=0):
+    r = np.zeros(48, np.float32)
+    r[0:3], r[3] = pos, radius
+    q = np.asarray(quat, np.float64)
+    r[4:8] = q / np.linalg.norm(q)
+    r[8:11], r[11] = vel, 0.5
+    r[12:15] = angvel
+    r[32:35], r[35] = size, shape
+    r[36] = mass
+    r[44:48] = np.array([group, mask, flags, 0], np.uint32).view(np.float32)
+    return r
+
+
+def couple_case(ref, kern, mods):
+    cmods, (cshared, ccode), acode = coupling_sources(ref)
+    g, rec, mats, dt = scene_records(16, [({"box": [[0.2, 0.2, 0.2], [0.8, 0.5, 0.8]]},
+                                           dict(kind=0, density=1, stiffness=1.0, viscosity=0.0), [0, 0, 0])])
+    rec = randomise(rec, 11, scale=0.5)
+    vol4 = np.float32(4 * (1 / 2 ** 3))
+    gs = p2g(kern, mods, rec, g["dims"], mats, vol4, False)
+    grav = [np.float32(0), np.float32((-9.81 * dt * dt) / g["dx"]), np.float32(0)]
+    gv = grid_update(kern, mods, gs, g["dims"], grav, np.zeros((16, 12), np.float32), 0)
+    s30 = np.sin(np.pi / 12)
+    bodies = np.stack([
+        body_record([0.5, 0.35, 0.5], [0, 0, 0, 1], [0.1, -0.2, 0], [0, 0, 1.0], 0, [0.1, 0.1, 0.1], 2.0, 0.1),
+        body_record([0.35, 0.3, 0.4], [0.2, 0.3, 0.1, 0.93], [0, 0, 0.3], [1.0, 0, 0], 1, [0.08, 0.05, 0.1], 1.0, 0.137),
+        body_record([0.65, 0.3, 0.62], [0, 0, s30, np.cos(np.pi / 12)], [0, 0, 0], [0, 0, 0], 2, [0.05, 0.08, 0.05], 0.0, 0.13),
+        body_record([0.3, 0.4, 0.7], [0, 0, 0, 1], [0, 0, 0], [0, 0, 0], 0, [0.06, 0.06, 0.06], 1.0, 0.06, flags=4),
+        body_record([0.7, 0.4, 0.3], [0, 0, 0, 1], [0, 0, 0], [0, 0, 0], 0, [0.06, 0.06, 0.06], 1.0, 0.06, group=2)])
+    dts, dx = float(dt), float(g["dx"])
+    prm = {"nBodies": np.uint32(len(bodies)), "mask": np.uint32(1), "origin": W.Vec(np.zeros(3, np.float32)),
+           "dx": np.float32(dx), "invDx": np.float32(1 / dx), "lead": np.float32(1.5 * dts),
+           "velToLattice": np.float32(dts / dx), "friction": np.float32(0.2), "band": np.float32(0.5)}
+    dims = g["dims"]
+    consts = f"const WG = 64u;\nconst DIMS = vec3u({dims[0]}u, {dims[1]}u, {dims[2]}u);\n"
+    ns = W.compile_module(consts + cmods + "\n" + cshared, "let wgi = wid.x + wid.y * nwg.x;\nlet p = gid;\n" + ccode)
+    grid = W.Buffer(gv.copy(), "i32", 4)
+    gacc = W.Buffer(np.zeros(len(bodies) * 8, np.int32), "i32", 1)
+    B = W.Buffer(bodies.copy(), "f32", 48, struct=BODY_FIELDS, struct_types={"info": "u32"})
+    W.dispatch3(ns, [math.ceil(d / 4) for d in dims], (4, 4, 4), {"grid": grid, "B": B, "gacc": gacc}, prm)
+    acc = gacc.arr.copy()
+    ns2 = W.compile_module(f"const WG = {WG}u;\n" + cmods, "let i = wgi * WG + lidx;\nif (i >= u.n) { return; }\n" + acode)
+    ext = W.Buffer(np.zeros((len(bodies) * 2, 4), np.float32), "f32", 4)
+    accb = W.Buffer(acc.reshape(-1, 4).copy(), "i32", 4)
+    m2w = np.float32(1.0 * dx ** 4 / dts)
+    W.dispatch(ns2, 1, WG, {"acc": accb, "ext": ext}, {"n": np.uint32(len(bodies)), "momToWorld": m2w, "dx": np.float32(dx)})
+    return {"rec": rec, "mats": mats, "dims": np.array(dims), "grid_in": gv, "bodies": bodies,
+            "params": np.array([0, 0, 0, dx, 1 / dx, 1.5 * dts, dts / dx, 0.2, 0.5], np.float32), "mask": 1,
+            "grid_out": grid.arr.copy(), "acc": acc, "mom_to_world": m2w, "ext": ext.arr.reshape(-1, 8).copy()}
+
+
+def main_couple(ref):
+    mods, kern = kernel_sources(ref)
+    out = couple_case(ref, kern, mods)
+    np.savez_compressed(os.path.join(HERE, "couple.npz"), **out)
+    moved = int((out["grid_out"] != out["grid_in"]).any(1).sum())
+    print("couple", moved, "nodes changed; acc", out["acc"].reshape(-1, 8)[:, [0, 1, 2, 4, 5, 6]].tolist())
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref_dir = next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")
+    if "--couple" in sys.argv:
+        main_couple(ref_dir)
+    else:
+        main(ref_dir)
+        main_couple(ref_dir)

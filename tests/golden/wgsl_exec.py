@@ -120,6 +120,9 @@ class Vec:
     def __truediv__(self, o): return Vec(wdiv(self.a, self._b(o)))
     def __rtruediv__(self, o): return Vec(wdiv(self._b(o), self.a))
     def __neg__(self): return Vec(-self.a)
+    def __eq__(self, o): return Vec(self.a == self._b(o))
+    def __ne__(self, o): return Vec(self.a != self._b(o))
+    __hash__ = None
     def __lt__(self, o): return Vec(self.a < self._b(o))
     def __le__(self, o): return Vec(self.a <= self._b(o))
     def __gt__(self, o): return Vec(self.a > self._b(o))
@@ -241,14 +244,16 @@ def concrete(v):
 class Buffer:
     """A storage buffer: numpy array (N, width) of f32/i32/u32 elements, or struct rows."""
 
-    def __init__(self, arr, kind, width=1, struct=None):
+    def __init__(self, arr, kind, width=1, struct=None, struct_types=None):
         self.arr, self.kind, self.width, self.struct = arr, kind, width, struct
+        self.struct_types = struct_types or {}
 
     def __getitem__(self, idx):
         idx = int(idx)
         if self.struct:
             row = self.arr[idx]
-            return types.SimpleNamespace(**{n: Vec(row[4 * k:4 * k + 4].copy()) for k, n in enumerate(self.struct)})
+            return types.SimpleNamespace(**{n: Vec(row[4 * k:4 * k + 4].copy().view(
+                {"u32": u32, "i32": i32}.get(self.struct_types.get(n), row.dtype))) for k, n in enumerate(self.struct)})
         if self.width == 1:
             return self.arr[idx]
         return Vec(self.arr[idx].copy())
@@ -257,7 +262,7 @@ class Buffer:
         idx = int(idx)
         if self.struct:
             for k, n in enumerate(self.struct):
-                self.arr[idx, 4 * k:4 * k + 4] = getattr(v, n).a
+                self.arr[idx, 4 * k:4 * k + 4] = getattr(v, n).a.view(self.arr.dtype)
         elif self.width == 1:
             self.arr[idx] = v
         else:
@@ -708,7 +713,10 @@ def compile_module(src, entry_body=None):
         g.boxed = set()
         addressed(body, g.boxed)
         g.boxed -= shared_names
-        g.emit("def main(lidx, wgi):", 0)
+        g.emit("def main(lidx, wgi, wid=None, lid=None, gid=None, nwg=None):", 0)
+        scalars = [n for n, ty in shared_decls if ty[0] != "array"]
+        if scalars:
+            g.emit("global " + ", ".join(scalars), 1)
         g.stmts(body, 1)
         if not has_barrier(body):
             g.emit("yield", 1)    # every entry is a generator
@@ -910,7 +918,8 @@ RUNTIME = {
     "log": _map(lambda x: f32(np.log(f32(x)))), "exp": _map(lambda x: f32(np.exp(f32(x)))),
     "max": _map(_fmax), "min": _map(_fmin), "clamp": _map(_clamp), "dot": _dot, "length": _length,
     "normalize": _normalize, "cross": _cross, "transpose": _transpose, "determinant": _determinant,
-    "select": _select, "any": _any, "bitcast": bitcast, "atomicAdd": atomicAdd, "atomicMin": atomicMin,
+    "select": _select, "any": _any, "all": lambda v: bool(np.all(v.a)) if isinstance(v, Vec) else bool(v),
+    "sign": _map(lambda x: type(x)(np.sign(x))), "bitcast": bitcast, "atomicAdd": atomicAdd, "atomicMin": atomicMin,
     "atomicMax": atomicMax, "atomicLoad": atomicLoad, "atomicStore": atomicStore,
 }
 RUNTIME["f32"] = _conv(f32)
@@ -936,3 +945,32 @@ def dispatch(ns, groups, wg, bindings, uniforms):
                     next(x[0])
                 except StopIteration:
                     x[1] = True
+
+
+def dispatch3(ns, groups, wg, bindings, uniforms):
+    """As dispatch, for a 3-D grid of workgroups of shape wg (local_invocation_index = x + wx (y + wy z))."""
+    ns["u"] = types.SimpleNamespace(**uniforms)
+    ns.update(bindings)
+    main = ns["main"]
+    nwg = Vec(np.array(groups, u32))
+    size = wg[0] * wg[1] * wg[2]
+    for gz in range(groups[2]):
+        for gy in range(groups[1]):
+            for gx in range(groups[0]):
+                for name, ty in ns["__shared_decls__"]:
+                    ns[name] = zero(ty)
+                wid = np.array([gx, gy, gz], u32)
+                live = []
+                for li in range(size):
+                    lid = np.array([li % wg[0], (li // wg[0]) % wg[1], li // (wg[0] * wg[1])], u32)
+                    gid = wid * np.array(wg, u32) + lid
+                    live.append([main(u32(li), u32(gx + gy * groups[0]), Vec(wid.copy()), Vec(lid),
+                                      Vec(gid), nwg), False])
+                while any(not x[1] for x in live):
+                    for x in live:
+                        if x[1]:
+                            continue
+                        try:
+                            next(x[0])
+                        except StopIteration:
+                            x[1] = True

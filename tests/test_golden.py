@@ -8,6 +8,8 @@ What the fixtures hold (tests/golden/gen_golden.py makes them, with the referenc
   g2p.npz         water, honey, jelly, snow and sand from a deformed state: mpm-p2g, mpm-grid, mpm-g2p
   sort.npz        mpm-key + scan + mpm-reorder of a shuffled scene at grid 32
   trajectory.npz  12 substeps of step()'s schedule (sort every 4th) for water and honey
+  couple.npz      the fluid <-> rigid coupling pass and apply (src/physics/coupling.js) on a pool with
+                  five bodies (dynamic sphere and rotated box, static capsule, disabled, masked out)
 
 Bar: bit-exact for keys, starts, sorted records, grid sums, the grid update and every particle
 field whose computation has no log/exp. log and exp are implementation-defined in WGSL (absolute
@@ -192,3 +194,18 @@ def test_cuda_substeps_match_reference_wgsl():
     sim.step(dt=sim.substepDt, K=int(d["substeps"]))
     assert np.array_equal(bits(sim.readParticles()), bits(d["out"]))
     sim.destroy()
+
+
+def test_oracle_coupling_matches_reference_wgsl():
+    """mpm-rigid-couple + mpm-rigid-apply (src/physics/coupling.js:83-196) on a water pool with a
+    dynamic sphere, a rotated dynamic box, a static capsule, a disabled and a masked-out body."""
+    d = fixture("couple.npz")
+    g, acc = O.couple(d["grid_in"], d["dims"], d["bodies"], d["params"], int(d["mask"]))
+    assert np.array_equal(g, d["grid_out"])
+    assert np.array_equal(acc, d["acc"])
+    assert (g != d["grid_in"]).any(1).sum() > 20                   # the pass changed nodes
+    nz = d["acc"].reshape(-1, 8)[:, [0, 1, 2, 4, 5, 6]].any(1)
+    assert nz.tolist() == [True, True, False, False, False]        # static, disabled, masked: none
+    ext, rest = O.couple_apply(acc, len(d["bodies"]), float(d["mom_to_world"]), float(d["params"][3]))
+    assert np.array_equal(bits(ext), bits(d["ext"]))
+    assert not rest.any()
