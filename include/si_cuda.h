@@ -192,6 +192,14 @@ int si_collider_row(const si_mpm* h, int32_t type, const double center[3], const
                     double radius, double friction, const double velocity[3], double substep_dt,
                     float row[12]);
 
+/* add(shape, opts) with the sampling on the device (mpm.js:207-232, sampleShape mpm.js:683-714):
+ * shape 0 box (a = lo, b = hi), 1 sphere (a = centre, radius), 2 cylinder (a = centre, radius,
+ * half_height), world units; lattice spacing dx / ppcAxis; xorshift32 jitter from `seed`
+ * (0 -> 1); `material` is the slot of set_materials; truncated at maxParticles. The records equal,
+ * bit for bit, si_sample_shape + si_make_records + si_mpm_add_particles. *added = particles added. */
+int si_mpm_emit(si_mpm* h, int32_t shape, const double a[3], const double b[3], double radius, double half_height,
+                double jitter, uint32_t seed, int32_t material, const double velocity[3], int64_t* added);
+
 /* ---------------------------------------------------------------- fluid <-> rigid coupling
  * MPM.couple(world, o) / uncouple() (mpm.js:244-259, src/physics/coupling.js:62-222): rigid bodies
  * become moving boundaries of the grid. `bodies` is n records of 48 floats, the reference's Body

@@ -22,7 +22,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["si_kernels.cu", "si_sort.cu", "si_couple.cu"]
+CU_SOURCES = ["si_kernels.cu", "si_sort.cu", "si_couple.cu", "si_emit.cu"]
 CPP_SOURCES = ["si_runtime.cpp", "si_host.cpp", "si_server.cpp"]
 
 

@@ -25,6 +25,7 @@
 
 #include "si_cuda.h"
 #include "si_device.h"
+#include "si_emit.h"
 #include "si_internal.h"
 #include "si_runtime.h"
 
@@ -853,6 +854,93 @@ int si_mpm_add_particles(si_mpm* h, const float* rec, int64_t n, int64_t* added)
   if (n <= 0) return SI_OK;
   int r = put_records(h, rec, h->count, n);
   if (r) return r;
+  h->count += n;
+  invalidate(h);
+  world_free_graphs(h->w);
+  if (added) *added = n;
+  return SI_OK;
+}
+
+// One xorshift32 step (sampleShape's rand(), mpm.js:685) and its GF(2) matrix powers.
+static uint32_t xs_step_host(uint32_t s) {
+  s ^= s << 13;
+  s ^= s >> 17;
+  s ^= s << 5;
+  return s;
+}
+static uint32_t gf2_apply_host(const uint32_t* cols, uint32_t v) {
+  uint32_t r = 0;
+  for (int j = 0; j < 32; j++)
+    if ((v >> j) & 1u) r ^= cols[j];
+  return r;
+}
+
+int si_mpm_emit(si_mpm* h, int32_t shape, const double a[3], const double b[3], double radius, double half_height,
+                double jitter, uint32_t seed, int32_t material, const double velocity[3], int64_t* added) {
+  if (added) *added = 0;
+  GUARD(h);
+  if (!a || (shape == 0 && !b)) return si_fail(SI_EINVAL, "MPM.add: shape needs box | sphere | cylinder");
+  if (shape < 0 || shape > 2) return si_fail(SI_EINVAL, "MPM.add: shape needs box | sphere | cylinder | sdf | points");
+  if (material < 0 || material >= std::max(1, h->nmats)) return si_fail(SI_EINVAL, "MPM.add: unknown material slot");
+  EmitInfo e;
+  std::memset(&e, 0, sizeof(e));
+  const double spacing = h->dx / h->ppc_axis;
+  double lo[3], hi[3];
+  if (shape == 0) {
+    for (int k = 0; k < 3; k++) { lo[k] = a[k]; hi[k] = b[k]; }
+  } else if (shape == 1) {
+    for (int k = 0; k < 3; k++) { lo[k] = a[k] - radius; hi[k] = a[k] + radius; }
+  } else {
+    lo[0] = a[0] - radius; lo[1] = a[1] - half_height; lo[2] = a[2] - radius;
+    hi[0] = a[0] + radius; hi[1] = a[1] + half_height; hi[2] = a[2] + radius;
+  }
+  e.total = 1;
+  for (int k = 0; k < 3; k++) {
+    const double q = std::floor((hi[k] - lo[k]) / spacing);
+    e.n[k] = (int64_t)std::max(1.0, q);
+    e.total *= e.n[k];
+    e.lo[k] = lo[k];
+    e.a[k] = a[k];
+    e.origin[k] = h->origin[k];
+    e.hi[k] = (double)(h->dims[k] - h->bound);
+  }
+  if (e.total > (int64_t)1 << 31) return si_fail(SI_EINVAL, "MPM.add: more than 2^31 lattice points");
+  const int64_t room = h->cap - h->count;   // mpm.js:211
+  if (room <= 0) return SI_OK;
+  e.shape = shape;
+  e.r = radius;
+  e.spacing = spacing;
+  e.jitter = jitter;
+  e.seed = seed ? seed : 1u;
+  uint32_t m[32];
+  for (int j = 0; j < 32; j++) m[j] = xs_step_host(1u << j);
+  uint32_t m2[32];
+  for (int j = 0; j < 32; j++) m2[j] = gf2_apply_host(m, m[j]);
+  for (int j = 0; j < 32; j++) e.jump[0][j] = gf2_apply_host(m, m2[j]);          // M^3
+  for (int i = 1; i < 32; i++)
+    for (int j = 0; j < 32; j++) e.jump[i][j] = gf2_apply_host(e.jump[i - 1], e.jump[i - 1][j]);
+  e.dx = h->dx;
+  e.bound = (double)h->bound;
+  const double s = h->dt / h->dx;
+  for (int k = 0; k < 3; k++) e.vel[k] = (float)((velocity ? velocity[k] : 0.0) * s);
+  e.material = (uint32_t)material;
+  e.P = h->pbuf[h->pcur];
+  e.cap = h->cap;
+  e.offset = h->count;
+  e.room = room;
+  const int64_t ctas = (e.total + 255) / 256;
+  uint32_t* scratch = nullptr;
+  cudaStream_t st = h->w->st;
+  CK(cudaMallocAsync((void**)&scratch, (size_t)(ctas + 1) * 4, st));
+  if (launch_emit(e, scratch, st) != 0) {
+    cudaFreeAsync(scratch, st);
+    return si_fail(SI_EDEVICE, "MPM.add: emission launch failed");
+  }
+  uint32_t inside = 0;
+  CK(cudaMemcpyAsync(&inside, scratch + ctas, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaFreeAsync(scratch, st));
+  CK(cudaStreamSynchronize(st));
+  const int64_t n = std::min<int64_t>(inside, room);
   h->count += n;
   invalidate(h);
   world_free_graphs(h->w);

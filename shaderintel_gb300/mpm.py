@@ -308,13 +308,26 @@ class MPM:
         mat = self._material(o.get("material") or shape.get("material") or "water")
         vel = o.get("velocity") or shape.get("velocity") or [0, 0, 0]
         count = self.count
+        jitter, seed = o.get("jitter"), o.get("seed")
+        jitter = 0.6 if jitter is None else float(jitter)
+        seed = (count + 1 if seed is None else int(seed)) & 0xFFFFFFFF
+        if not o.get("_host") and any(k in shape for k in ("box", "sphere", "cylinder")) and "points" not in shape:
+            # sampled on the device: the same records as the host path below, bit for bit
+            if "box" in shape:
+                k, a, b, r, h = 0, shape["box"][0], shape["box"][1], 0.0, 0.0
+            elif "sphere" in shape:
+                k, a, b, r, h = 1, shape["sphere"][0], (0, 0, 0), float(shape["sphere"][1]), 0.0
+            else:
+                c, r, h = shape["cylinder"]
+                k, a, b = 2, c, (0, 0, 0)
+            added = ctypes.c_int64()
+            check(L.lib().si_mpm_emit(self._h, k, dptr(a), dptr(b), float(r), float(h), jitter, seed, mat, dptr(vel),
+                                      ctypes.byref(added)))
+            return added.value
         if "points" in shape and shape["points"] is not None:
             pts = np.asarray(shape["points"], np.float32).reshape(-1, 3)
         else:
-            jitter = o.get("jitter")
-            seed = o.get("seed")
-            pts = sample_shape(shape, self.dx / self.ppcAxis, 0.6 if jitter is None else jitter,
-                               count + 1 if seed is None else seed)
+            pts = sample_shape(shape, self.dx / self.ppcAxis, jitter, seed)
         n = min(len(pts), self.maxParticles - count)
         if n <= 0:
             return 0
