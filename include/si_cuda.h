@@ -44,6 +44,7 @@ extern "C" {
 typedef struct si_world si_world;   /* a CUDA stream + the scenes stepped together on it */
 typedef struct si_mpm si_mpm;       /* one simulation (the reference's MPM object) */
 typedef struct si_server si_server; /* continuous-batching request loop over one world */
+typedef struct si_spatial si_spatial; /* a uniform-grid neighbour binning (SpatialGrid) */
 
 /* Constructor options of `new MPM(ctx, o)`, mpm.js:89-109 (defaults by si_mpm_desc_default). */
 typedef struct si_mpm_desc {
@@ -217,6 +218,27 @@ int si_mpm_set_bodies(si_mpm* h, const float* bodies, int32_t n);
  * last read, in world units, n x 8 floats (J xyz, 0, L xyz, 0) — what the reference adds to the
  * rigid world's external impulses; the sums restart from zero. */
 int si_mpm_read_impulses(si_mpm* h, float* out, int32_t n);
+
+/* ---------------------------------------------------------------- SpatialGrid (src/prims/grid.js)
+ * Counting-sort binning of points into a uniform grid, the prim the MPM block sort specialises:
+ * new SpatialGrid(ctx, {maxCount, min, max, cellSize}) (grid.js:25-55): dims = max(1,
+ * ceil((max - min) / cellSize)) per axis, at most 2^26 cells. build(pos, count) (grid.js:69-76):
+ * cell = gridIndex(gridCoord(p)) (grid.js:14-20, x fastest, clamped to the grid), order = point
+ * indices sorted by cell, start = first sorted slot of every cell (numCells + 1 entries). Within a
+ * cell the reference ranks by atomic arrival (any order); here by index (stable, deterministic).
+ * Calls take the world's lock and run on its stream. */
+int si_spatial_create(si_world* w, int64_t max_count, const double min[3], const double max[3], double cell_size,
+                      si_spatial** out);
+int si_spatial_destroy(si_spatial* g);
+int si_spatial_info(const si_spatial* g, int32_t dims[3], int64_t* num_cells, int64_t* count);
+/* pos: count x 4 floats (vec4f, xyz used), host memory */
+int si_spatial_build(si_spatial* g, const float* pos, int64_t count);
+/* the same over an MPM scene's current particle positions (lattice units), without a copy */
+int si_spatial_build_mpm(si_spatial* g, const si_mpm* h);
+/* order (count u32) and start (numCells + 1 u32) of the last build; either may be NULL */
+int si_spatial_read(si_spatial* g, uint32_t* order, uint32_t* start);
+/* gather(src, dst), grid.js:79-90: dst[k] = src[order[k]] for `width` floats per point, host arrays */
+int si_spatial_gather(si_spatial* g, const float* src, float* dst, int32_t width);
 
 /* ---------------------------------------------------------------- serving
  * A request loop that keeps every scene resident in HBM and runs step(dt, K) requests by

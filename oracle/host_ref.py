@@ -146,3 +146,19 @@ def collider_row(c, dx, origin, substep_dt):
     for a in range(3):
         row[8 + a] = np.float32(v[a] * s)
     return row
+
+
+def spatial_grid(pos, origin, cell_size, dims):
+    """SpatialGrid.build of src/prims/grid.js:14-20, 69-76 in numpy (f32 cell arithmetic): cells,
+    order (stable: index order within a cell) and start (numCells + 1)."""
+    p = np.asarray(pos, np.float32)[:, :3]
+    o = np.asarray(origin, np.float32)
+    inv = np.float32(1.0 / cell_size)
+    c = np.floor((p - o) * inv)
+    c = np.clip(c, -2 ** 31, 2 ** 31 - 1).astype(np.int64)
+    c = np.minimum(np.maximum(c, 0), np.asarray(dims) - 1)
+    cell = (c[:, 0] + dims[0] * (c[:, 1] + dims[1] * c[:, 2])).astype(np.uint32)
+    order = np.argsort(cell, kind="stable").astype(np.uint32)
+    n_cells = int(dims[0]) * int(dims[1]) * int(dims[2])
+    start = np.searchsorted(cell[order], np.arange(n_cells + 1), side="left").astype(np.uint32)
+    return cell, order, start

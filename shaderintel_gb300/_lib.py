@@ -102,6 +102,14 @@ SIGNATURES = {
                                      ctypes.c_double]),
     "si_mpm_set_bodies": (ctypes.c_int, [vp, c_float_p, ctypes.c_int32]),
     "si_mpm_read_impulses": (ctypes.c_int, [vp, c_float_p, ctypes.c_int32]),
+    "si_spatial_create": (ctypes.c_int, [vp, ctypes.c_int64, c_double_p, c_double_p, ctypes.c_double,
+                                         ctypes.POINTER(vp)]),
+    "si_spatial_destroy": (ctypes.c_int, [vp]),
+    "si_spatial_info": (ctypes.c_int, [vp, c_int32_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "si_spatial_build": (ctypes.c_int, [vp, c_float_p, ctypes.c_int64]),
+    "si_spatial_build_mpm": (ctypes.c_int, [vp, vp]),
+    "si_spatial_read": (ctypes.c_int, [vp, c_uint32_p, c_uint32_p]),
+    "si_spatial_gather": (ctypes.c_int, [vp, c_float_p, c_float_p, ctypes.c_int32]),
     "si_server_create": (ctypes.c_int, [vp, ctypes.c_int64, ctypes.POINTER(vp)]),
     "si_server_destroy": (ctypes.c_int, [vp]),
     "si_server_admit": (ctypes.c_int, [vp, ctypes.POINTER(si_mpm_desc), ctypes.POINTER(vp)]),

@@ -326,3 +326,208 @@ extern "C" int si_block_sort_noalloc(const float* x, int64_t stride_floats, int3
   }
   return cudaGetLastError() == cudaSuccess ? SI_OK : si_fail_c(SI_EDEVICE, "si_block_sort_noalloc: launch failed");
 }
+
+// ------------------------------------------------------------------ SpatialGrid (src/prims/grid.js)
+// Uniform-grid neighbour binning of arbitrary points: cell = gridIndex(gridCoord(p)) (grid.js:14-20,
+// x-fastest), then the same stable radix sort as the block sort, and start[] = the first sorted slot
+// of every cell (numCells + 1 entries). The reference ranks points within a cell by atomic arrival
+// (any order); the stable sort keeps them in index order, one of those orders, always the same.
+#include "si_runtime.h"
+
+struct si_spatial {
+  si_world* w = nullptr;
+  int64_t max_count = 0, count = 0;
+  int32_t dims[3] = {1, 1, 1};
+  uint32_t cells = 1;
+  float origin[3] = {0, 0, 0};
+  float inv = 1.0f;
+  uint32_t *ka = nullptr, *va = nullptr, *kb = nullptr, *vb = nullptr, *hist = nullptr, *digit_total = nullptr;
+  uint32_t* start = nullptr;
+  uint32_t* order = nullptr;   // points to va or vb after a build
+  float4* pos = nullptr;       // staging of host positions
+  bool destroyed = false;
+};
+
+namespace si {
+// gridCoord + gridIndex, grid.js:14-20: clamp(vec3i(floor((p - origin) * inv)), 0, dims - 1)
+__global__ void k_spatial_cells(const float4* __restrict__ pos, int64_t n, float o0, float o1, float o2, float inv,
+                                int32_t d0, int32_t d1, int32_t d2, uint32_t* keys, uint32_t* vals) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 p = pos[i];
+    const int32_t cx = min(max(__float2int_rz(floorf((p.x - o0) * inv)), 0), d0 - 1);
+    const int32_t cy = min(max(__float2int_rz(floorf((p.y - o1) * inv)), 0), d1 - 1);
+    const int32_t cz = min(max(__float2int_rz(floorf((p.z - o2) * inv)), 0), d2 - 1);
+    keys[i] = (uint32_t)cx + (uint32_t)d0 * ((uint32_t)cy + (uint32_t)d1 * (uint32_t)cz);
+    vals[i] = (uint32_t)i;
+  }
+}
+
+__global__ void k_spatial_gather(const float* __restrict__ src, float* dst, const uint32_t* __restrict__ order,
+                                 int64_t n, int32_t width) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * width; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = t / width;
+    dst[t] = src[(int64_t)order[k] * width + (t - k * width)];
+  }
+}
+}  // namespace si
+
+static int spatial_sort(si_spatial* g, const float4* pos, int64_t n) {
+  using namespace si;
+  cudaStream_t st = g->w->st;
+  g->count = n;
+  if (n > 0) {
+    const unsigned ctas = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
+    k_spatial_cells<<<ctas, 256, 0, st>>>(pos, n, g->origin[0], g->origin[1], g->origin[2], g->inv, g->dims[0],
+                                          g->dims[1], g->dims[2], g->ka, g->va);
+    int bits = 1;
+    while (bits < 32 && (1ull << bits) < (uint64_t)std::max<uint32_t>(g->cells, 2u)) bits++;
+    const int passes = (bits + kRadixBits - 1) / kRadixBits;
+    const uint32_t tiles = ((uint32_t)n + kSortTile - 1) / kSortTile;
+    uint32_t *ka = g->ka, *va = g->va, *kb = g->kb, *vb = g->vb;
+    for (int p = 0; p < passes; p++) {
+      k_radix_hist<<<tiles, kCtaThreads, 0, st>>>(ka, (uint32_t)n, p * kRadixBits, g->hist, tiles);
+      k_radix_scan<<<256, kCtaThreads, 0, st>>>(g->hist, tiles, g->digit_total);
+      k_radix_scatter<<<tiles, kCtaThreads, 0, st>>>(ka, va, kb, vb, (uint32_t)n, p * kRadixBits, g->hist,
+                                                     g->digit_total, tiles);
+      std::swap(ka, kb);
+      std::swap(va, vb);
+    }
+    g->order = va;
+    k_na_starts<<<(unsigned)std::min<uint64_t>(((uint64_t)g->cells + 256) / 256, 65535), 256, 0, st>>>(
+        ka, (int32_t)n, g->cells, g->start);
+  } else {
+    g->order = g->va;
+    k_na_starts<<<(unsigned)std::min<uint64_t>(((uint64_t)g->cells + 256) / 256, 65535), 256, 0, st>>>(
+        g->ka, 0, g->cells, g->start);
+  }
+  return cudaGetLastError() == cudaSuccess ? SI_OK : si_fail_c(SI_EDEVICE, "SpatialGrid.build: launch failed");
+}
+
+#define SG_GUARD(g)                                                                     \
+  if (!(g)) return si_fail_c(SI_EINVAL, "null SpatialGrid");                            \
+  std::lock_guard<std::recursive_mutex> sg_lock_((g)->w->api_mu);                       \
+  if ((g)->destroyed || (g)->w->destroyed) return si_fail_c(SI_EDESTROYED, "SpatialGrid: it was destroyed")
+
+extern "C" {
+
+int si_spatial_create(si_world* w, int64_t max_count, const double mn[3], const double mx[3], double cell_size,
+                      si_spatial** out) {
+  if (!w || !mn || !mx || !out) return si_fail_c(SI_EINVAL, "SpatialGrid: null argument");
+  if (max_count < 0 || max_count > ((int64_t)1 << 31) - 1) return si_fail_c(SI_EINVAL, "SpatialGrid: bad maxCount");
+  if (!(cell_size > 0)) return si_fail_c(SI_EINVAL, "SpatialGrid: cellSize must be > 0");
+  std::lock_guard<std::recursive_mutex> lock(w->api_mu);
+  if (w->destroyed) return si_fail_c(SI_EDESTROYED, "the world was destroyed");
+  auto* g = new si_spatial();
+  g->w = w;
+  g->max_count = max_count;
+  uint64_t cells = 1;
+  for (int a = 0; a < 3; a++) {   // grid.js:31-33
+    g->dims[a] = (int32_t)std::max(1.0, std::ceil((mx[a] - mn[a]) / cell_size));
+    g->origin[a] = (float)mn[a];
+    cells *= (uint64_t)g->dims[a];
+  }
+  if (cells > (1u << 26)) {
+    delete g;
+    return si_fail_c(SI_EINVAL, "SpatialGrid: too many cells; increase cellSize");
+  }
+  g->cells = (uint32_t)cells;
+  g->inv = (float)(1.0 / cell_size);
+  cudaStream_t st = w->st;
+  const size_t n = (size_t)std::max<int64_t>(max_count, 1);
+  const size_t tiles = (n + si::kSortTile - 1) / si::kSortTile;
+  cudaError_t e = cudaSuccess;
+  for (uint32_t** p : {&g->ka, &g->va, &g->kb, &g->vb})
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)p, n * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&g->hist, 256 * tiles * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&g->digit_total, 256 * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&g->start, ((size_t)cells + 1) * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&g->pos, n * 16, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->start, 0, ((size_t)cells + 1) * 4, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    for (void* p : {(void*)g->ka, (void*)g->va, (void*)g->kb, (void*)g->vb, (void*)g->hist, (void*)g->digit_total,
+                    (void*)g->start, (void*)g->pos})
+      if (p) cudaFreeAsync(p, st);
+    delete g;
+    return si_fail_c(e == cudaErrorMemoryAllocation ? SI_ENOMEM : SI_EDEVICE, "SpatialGrid: device allocation failed");
+  }
+  g->order = g->va;
+  *out = g;
+  return SI_OK;
+}
+
+int si_spatial_destroy(si_spatial* g) {
+  if (!g) return si_fail_c(SI_EINVAL, "null SpatialGrid");
+  {
+    std::lock_guard<std::recursive_mutex> lock(g->w->api_mu);
+    if (!g->destroyed && !g->w->destroyed) {
+      for (void* p : {(void*)g->ka, (void*)g->va, (void*)g->kb, (void*)g->vb, (void*)g->hist, (void*)g->digit_total,
+                      (void*)g->start, (void*)g->pos})
+        if (p) cudaFreeAsync(p, g->w->st);
+      cudaStreamSynchronize(g->w->st);
+    }
+    g->destroyed = true;
+  }
+  delete g;
+  return SI_OK;
+}
+
+int si_spatial_info(const si_spatial* g, int32_t dims[3], int64_t* num_cells, int64_t* count) {
+  if (!g) return si_fail_c(SI_EINVAL, "null SpatialGrid");
+  if (dims) for (int a = 0; a < 3; a++) dims[a] = g->dims[a];
+  if (num_cells) *num_cells = g->cells;
+  if (count) *count = g->count;
+  return SI_OK;
+}
+
+int si_spatial_build(si_spatial* g, const float* pos, int64_t count) {
+  SG_GUARD(g);
+  if (count < 0 || (count && !pos)) return si_fail_c(SI_EINVAL, "SpatialGrid.build: bad positions");
+  if (count > g->max_count) return si_fail_c(SI_EINVAL, "SpatialGrid.build: points exceed maxCount");
+  if (count && cudaMemcpyAsync(g->pos, pos, (size_t)count * 16, cudaMemcpyHostToDevice, g->w->st) != cudaSuccess)
+    return si_fail_c(SI_EDEVICE, "SpatialGrid.build: upload failed");
+  return spatial_sort(g, g->pos, count);
+}
+
+int si_spatial_build_mpm(si_spatial* g, const si_mpm* h) {
+  SG_GUARD(g);
+  if (!h || h->destroyed) return si_fail_c(SI_EINVAL, "SpatialGrid.build: no simulation");
+  if (h->w != g->w) return si_fail_c(SI_EINVAL, "SpatialGrid.build: the simulation belongs to another world");
+  if (h->count > g->max_count) return si_fail_c(SI_EINVAL, "SpatialGrid.build: points exceed maxCount");
+  return spatial_sort(g, h->pbuf[h->pcur], h->count);
+}
+
+int si_spatial_read(si_spatial* g, uint32_t* order, uint32_t* start) {
+  SG_GUARD(g);
+  cudaStream_t st = g->w->st;
+  if (order && g->count &&
+      cudaMemcpyAsync(order, g->order, (size_t)g->count * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return si_fail_c(SI_EDEVICE, "SpatialGrid: read failed");
+  if (start && cudaMemcpyAsync(start, g->start, ((size_t)g->cells + 1) * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return si_fail_c(SI_EDEVICE, "SpatialGrid: read failed");
+  return cudaStreamSynchronize(st) == cudaSuccess ? SI_OK : si_fail_c(SI_EDEVICE, "SpatialGrid: read failed");
+}
+
+int si_spatial_gather(si_spatial* g, const float* src, float* dst, int32_t width) {
+  SG_GUARD(g);
+  if (width <= 0 || (g->count && (!src || !dst))) return si_fail_c(SI_EINVAL, "SpatialGrid.gather: bad arguments");
+  if (!g->count) return SI_OK;
+  cudaStream_t st = g->w->st;
+  const size_t bytes = (size_t)g->count * (size_t)width * 4;
+  float *ds = nullptr, *dd = nullptr;
+  if (cudaMallocAsync((void**)&ds, bytes, st) != cudaSuccess || cudaMallocAsync((void**)&dd, bytes, st) != cudaSuccess) {
+    cudaGetLastError();
+    if (ds) cudaFreeAsync(ds, st);
+    return si_fail_c(SI_ENOMEM, "SpatialGrid.gather: device allocation failed");
+  }
+  cudaMemcpyAsync(ds, src, bytes, cudaMemcpyHostToDevice, st);
+  const int64_t total = g->count * width;
+  si::k_spatial_gather<<<(unsigned)std::min<int64_t>((total + 255) / 256, 8192), 256, 0, st>>>(ds, dd, g->order,
+                                                                                             g->count, width);
+  cudaMemcpyAsync(dst, dd, bytes, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(ds, st);
+  cudaFreeAsync(dd, st);
+  return cudaStreamSynchronize(st) == cudaSuccess ? SI_OK : si_fail_c(SI_EDEVICE, "SpatialGrid.gather failed");
+}
+
+}  // extern "C"
