@@ -121,6 +121,12 @@ int si_mpm_clear(si_mpm* h);
 int si_mpm_write_particles(si_mpm* h, const float* records, int64_t offset, int64_t n);
 int si_mpm_read_particles(si_mpm* h, float* records, int64_t offset, int64_t n);
 /* readPositions(), mpm.js:624-630: world xyz = x*dx + origin. */
+/* The instance buffer of the sphere layer (spheres(), mpm.js:658-679, vertex stage of
+ * src/render/spheres.js:50-60) without a renderer: per particle 8 floats — world x, y, z
+ * (x * dx + origin in f32, as the shader), radius (dx / ppcAxis * 0.6 * size, 0 when the material
+ * is not in mat_mask: the culled instance), world velocity (v * dx / dt in f32), material (u32 bits).
+ * mat_mask = ~fluidMask() gives spheres({solidsOnly: true}). */
+int si_mpm_read_instances(si_mpm* h, float* out, int64_t offset, int64_t n, uint32_t mat_mask, double size);
 int si_mpm_read_positions(si_mpm* h, float* xyz, int64_t offset, int64_t n);
 /* colBuf.writeOrdered of _uploadColliders, mpm.js:276-293: k <= 16 rows of 12 floats in lattice
  * units [kind(u32), center xyz, radius | half xyz | normal xyz, friction, velocity xyz (cells/substep), 0]. */

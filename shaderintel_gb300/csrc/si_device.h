@@ -112,6 +112,8 @@ void launch_keys(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_retime(float4* P, int64_t cap, int32_t n, float k, cudaStream_t st);
 void launch_aos_to_soa(const float* aos, float4* P, int64_t cap, int64_t off, int64_t n, cudaStream_t st);
 void launch_soa_to_aos(const float4* P, int64_t cap, int64_t off, int64_t n, float* aos, cudaStream_t st);
+void launch_instances(const float4* P, int64_t cap, int64_t off, int64_t n, float scale, const float offset[3],
+                      float radius, float vel_scale, uint32_t mat_mask, float* out, cudaStream_t st);
 void launch_positions(const float4* P, int64_t cap, int64_t off, int64_t n, double dx,
                       const double origin[3], float* xyz, cudaStream_t st);
 // Sort of one tick: builds the concatenated (key, index) arrays of the sorting scenes, radix

@@ -811,6 +811,20 @@ __global__ void k_positions(const float4* __restrict__ P, int64_t off, int64_t n
   }
 }
 
+// Instances of the sphere layer (spheres(), mpm.js:658-679; its vertex stage src/render/spheres.js:50-60)
+// as a headless buffer: world = x * scale + offset and v * velScale in f32 as the shader computes them,
+// the layer's radius, and a radius of 0 for a material the mask culls.
+__global__ void k_instances(const float4* __restrict__ P, int64_t cap, int64_t off, int64_t n, float scale, float o0,
+                            float o1, float o2, float radius, float vel_scale, uint32_t mat_mask, float4* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 x = P[off + i], v = P[cap + off + i];
+    const uint32_t mat = __float_as_uint(x.w);
+    const bool keep = ((mat_mask >> (mat & 31u)) & 1u) == 1u;
+    out[2 * i] = make_float4(x.x * scale + o0, x.y * scale + o1, x.z * scale + o2, keep ? radius : 0.0f);
+    out[2 * i + 1] = make_float4(v.x * vel_scale, v.y * vel_scale, v.z * vel_scale, x.w);
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 int p2g_smem_bytes(int tile_nodes, int ppt) {
   (void)tile_nodes;
@@ -884,6 +898,13 @@ void launch_soa_to_aos(const float4* P, int64_t cap, int64_t off, int64_t n, flo
   if (n <= 0) return;
   int ctas = (int)std::min<int64_t>((n * kStreams + 255) / 256, 8192);
   k_soa_to_aos<<<ctas, 256, 0, st>>>(P, cap, off, n, reinterpret_cast<float4*>(aos));
+}
+void launch_instances(const float4* P, int64_t cap, int64_t off, int64_t n, float scale, const float offset[3],
+                      float radius, float vel_scale, uint32_t mat_mask, float* out, cudaStream_t st) {
+  if (n <= 0) return;
+  int ctas = (int)std::min<int64_t>((n + 255) / 256, 8192);
+  k_instances<<<ctas, 256, 0, st>>>(P, cap, off, n, scale, offset[0], offset[1], offset[2], radius, vel_scale, mat_mask,
+                                    reinterpret_cast<float4*>(out));
 }
 void launch_positions(const float4* P, int64_t cap, int64_t off, int64_t n, double dx, const double origin[3],
                       float* xyz, cudaStream_t st) {

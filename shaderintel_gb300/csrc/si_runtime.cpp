@@ -999,6 +999,27 @@ int si_mpm_read_positions(si_mpm* h, float* xyz, int64_t off, int64_t n) {
   return SI_OK;
 }
 
+int si_mpm_read_instances(si_mpm* h, float* out, int64_t off, int64_t n, uint32_t mat_mask, double size) {
+  GUARD(h);
+  if (off < 0 || n < 0 || off + n > h->count || (n && !out))
+    return si_fail(SI_EINVAL, "MPM: read outside [0, count)");
+  if (n == 0) return SI_OK;
+  si_world* w = h->w;
+  // the layer's uniforms (mpm.js:662-664), JavaScript numbers written as f32
+  const float scale = (float)h->dx;
+  const float offset[3] = {(float)h->origin[0], (float)h->origin[1], (float)h->origin[2]};
+  const float radius = (float)((h->dx / h->ppc_axis) * 0.6 * size);
+  const float vel_scale = (float)(h->dx / h->dt);
+  float* stage = nullptr;
+  CK(cudaMallocAsync((void**)&stage, (size_t)n * 32, w->st));
+  launch_instances(h->pbuf[h->pcur], h->cap, off, n, scale, offset, radius, vel_scale, mat_mask, stage, w->st);
+  CK(cudaMemcpyAsync(out, stage, (size_t)n * 32, cudaMemcpyDeviceToHost, w->st));
+  CK(cudaFreeAsync(stage, w->st));
+  CK(cudaStreamSynchronize(w->st));
+  CK(cudaGetLastError());
+  return SI_OK;
+}
+
 int si_mpm_set_colliders(si_mpm* h, const float* rows, int32_t k) {
   GUARD(h);
   if (k < 0 || (k && !rows)) return si_fail(SI_EINVAL, "MPM: bad collider table");

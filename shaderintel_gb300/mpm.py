@@ -431,6 +431,19 @@ class MPM:
             check(L.lib().si_mpm_read_positions(self._h, fptr(out), 0, n))
         return out
 
+    def readInstances(self, solidsOnly=False, size=1.0, matMask=None):
+        """The sphere layer's instances as a headless buffer (spheres(), mpm.js:658-679): (count, 8)
+        float32 — world xyz, radius (0 = culled by the material mask), world velocity, material id
+        (u32 bits). solidsOnly culls the fluid materials like spheres({solidsOnly: true})."""
+        mask = (~self.fluidMask() & 0xFFFFFFFF) if solidsOnly else 0xFFFFFFFF
+        if matMask is not None:
+            mask = int(matMask) & 0xFFFFFFFF
+        n = self.count
+        out = np.empty((n, 8), np.float32)
+        if n:
+            check(L.lib().si_mpm_read_instances(self._h, fptr(out), 0, n, mask, float(size)))
+        return out
+
     def readParticles(self, offset=0, n=None):
         n = self.count - offset if n is None else n
         out = np.empty((n, 32), np.float32)

@@ -346,3 +346,27 @@ def test_capacity_truncates_add_and_empty_step_is_noop():
     sim.step()
     assert sim.stepCount == sim.substeps
     sim.destroy()
+
+
+def test_sphere_layer_instances_headless():
+    """spheres() / spheres({solidsOnly}) (mpm.js:658-679, src/render/spheres.js:50-60) as a buffer."""
+    sim = MPM(grid=32, maxParticles=60000, substeps=8, origin=[0.25, -0.5, 1.0])
+    sim.add({"box": [[0.3, 0.1, 0.3], [0.6, 0.4, 0.6]]}, material="water")
+    sim.add({"sphere": [[0.5, 0.7, 0.5], 0.1]}, material="jelly", velocity=[0, -1, 0])
+    sim.step()
+    P = sim.readParticles()
+    f = np.float32
+    dx, o = f(sim.dx), np.array(sim.origin, np.float32)
+    world = P[:, :3] * dx + o
+    vel = P[:, 4:7] * f(sim.dx / sim.substepDt)
+    radius = f((sim.dx / sim.ppcAxis) * 0.6)
+    inst = sim.readInstances()
+    assert np.array_equal(inst[:, :3].view(np.uint32), world.view(np.uint32))
+    assert np.array_equal(inst[:, 4:7].view(np.uint32), vel.view(np.uint32))
+    assert np.array_equal(inst[:, 7].view(np.uint32), P[:, 3].view(np.uint32))
+    assert (inst[:, 3] == radius).all()
+    solid = sim.readInstances(solidsOnly=True)
+    water = P[:, 3].view(np.uint32) == 0
+    assert sim.fluidMask() == 1
+    assert (solid[water, 3] == 0).all() and (solid[~water, 3] == radius).all()
+    sim.destroy()
