@@ -504,6 +504,21 @@ def run_reference(a):
     }
 
 
+def reduce_replicas(out, world_size, substeps):
+    """Independent replicas (one scene per GPU, no device collective): the job's time per step is
+    the maximum over ranks, its value the particle-substeps of all ranks over that time. Needs an
+    initialised process group (gloo: host tensors only)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([out["ms_per_step"]], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    out = dict(out)
+    out["ms_per_step"] = float(t[0])
+    out["value"] = out["config"]["particles"] * substeps * world_size / (float(t[0]) / 1e3)
+    out["config"] = dict(out["config"], parallelism=f"replicas x{world_size}")
+    return out
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -548,16 +563,17 @@ def main():
         out["batched"] = run_batched(a, log)
     if world_size == 1 and not a.no_served:
         out["served"] = run_served(a, log)
+        # the same loop offered more than it can run: its capacity (latency is then queueing)
+        import types
+        sat = types.SimpleNamespace(serve_rate=max(8000.0, 4 * a.serve_rate), serve_seconds=min(5.0, a.serve_seconds),
+                                    serve_resident=a.serve_resident)
+        out["served_saturated"] = run_served(sat, log)
     if world_size == 1:
         out["conservation"] = run_conservation()
-    if world_size > 1:   # independent replicas: the job value is the sum, the time the max over ranks
+    if world_size > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-        import torch
-        t = torch.tensor([out["ms_per_step"]], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        out["ms_per_step"] = float(t[0])
-        out["value"] = out["config"]["particles"] * CONFIGS[a.config]["substeps"] * world_size / (t[0].item() / 1e3)
+        out = reduce_replicas(out, world_size, CONFIGS[a.config]["substeps"])
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out))
