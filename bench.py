@@ -355,6 +355,7 @@ def run_served(a, log):
     retired after 500 substeps and replaced by new ones."""
     import collections
     import random
+    from shaderintel_gb300 import SIError
     from shaderintel_gb300.serving import Server
     rng = random.Random(77)
     spec_iter = iter(scene_specs(1 << 20, 9191))
@@ -369,7 +370,9 @@ def run_served(a, log):
         s = next(spec_iter)
         try:
             sim = srv.admit(grid=s["edge"], maxParticles=spec_capacity(s), substeps=8)
-        except Exception:
+        except SIError as e:
+            if e.code != "out-of-memory":   # only a full budget is an admission refusal
+                raise
             refused += 1
             return None
         fill_scene(sim, s)
