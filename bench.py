@@ -208,16 +208,26 @@ def run_ours(a, rank):
     peak, peak_kind = load_peaks()
     achieved = b_alg / (g2p_ms / 1e3) / 1e9
 
-    # end to end through the public API with host buffers
-    xyz, pinned = pinned_floats(n_p * 3)
+    # end to end through the public API with host buffers: every frame uploads the collider table and
+    # reads every position back, as readPositions()' Promise: frame k's positions are copied into one
+    # of two pinned buffers while frame k+1 runs, and the loop waits for frame k before queueing k+2
+    bufs = [pinned_floats(n_p * 3) for _ in range(2)]
+    pinned = bufs[0][1]
     cols, _ = pinned_floats(16 * 12)
     cols[:] = 0
     h = sim._h
+    ticket = ctypes.c_uint64()
+    pending = []
     t = time.perf_counter()
-    for _ in range(a.steps):
+    for k in range(a.steps):
         lib.si_mpm_set_colliders(h, L.fptr(cols), 0)   # the per-step collider table upload (mpm.js:586)
         L.check(lib.si_mpm_step(h, 0.0, 0))
-        L.check(lib.si_mpm_read_positions(h, L.fptr(xyz), 0, n_p))
+        if len(pending) == 2:
+            L.check(lib.si_mpm_read_wait(h, pending.pop(0)))
+        L.check(lib.si_mpm_read_positions_async(h, L.fptr(bufs[k % 2][0]), 0, n_p, ctypes.byref(ticket)))
+        pending.append(ticket.value)
+    for tk in pending:
+        L.check(lib.si_mpm_read_wait(h, tk))
     e2e_s = time.perf_counter() - t
     e2e = n_p * subs * a.steps / e2e_s
 

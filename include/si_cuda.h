@@ -128,6 +128,11 @@ int si_mpm_read_particles(si_mpm* h, float* records, int64_t offset, int64_t n);
  * mat_mask = ~fluidMask() gives spheres({solidsOnly: true}). */
 int si_mpm_read_instances(si_mpm* h, float* out, int64_t offset, int64_t n, uint32_t mat_mask, double size);
 int si_mpm_read_positions(si_mpm* h, float* xyz, int64_t offset, int64_t n);
+/* readPositions() as the reference's Promise (P.read, src/core/context.js:254-270): enqueues the
+ * copy into `xyz` behind the work already queued and returns at once with a ticket (with pinned host
+ * memory the copy runs while the host queues more steps); si_mpm_read_wait blocks until it landed. */
+int si_mpm_read_positions_async(si_mpm* h, float* xyz, int64_t offset, int64_t n, uint64_t* ticket);
+int si_mpm_read_wait(si_mpm* h, uint64_t ticket);
 /* colBuf.writeOrdered of _uploadColliders, mpm.js:276-293: k <= 16 rows of 12 floats in lattice
  * units [kind(u32), center xyz, radius | half xyz | normal xyz, friction, velocity xyz (cells/substep), 0]. */
 int si_mpm_set_colliders(si_mpm* h, const float* rows, int32_t k);

@@ -607,6 +607,13 @@ int si_world_destroy(si_world* w) {
   cudaStreamSynchronize(w->st);
   for (auto& e : w->pev) if (e) cudaEventDestroy(e);
   for (auto& e : w->marks) if (e) cudaEventDestroy(e);
+  if (w->st_copy) {
+    cudaStreamSynchronize(w->st_copy);
+    cudaStreamDestroy(w->st_copy);
+    w->st_copy = nullptr;
+  }
+  for (auto& kv : w->reads) cudaEventDestroy(kv.second);
+  w->reads.clear();
   cudaStreamDestroy(w->st);
   w->destroyed = true;
   return SI_OK;
@@ -1018,6 +1025,46 @@ int si_mpm_read_instances(si_mpm* h, float* out, int64_t off, int64_t n, uint32_
   CK(cudaStreamSynchronize(w->st));
   CK(cudaGetLastError());
   return SI_OK;
+}
+
+int si_mpm_read_positions_async(si_mpm* h, float* xyz, int64_t off, int64_t n, uint64_t* ticket) {
+  GUARD(h);
+  if (!ticket || off < 0 || n < 0 || off + n > h->count || (n && !xyz))
+    return si_fail(SI_EINVAL, "MPM: read outside [0, count)");
+  si_world* w = h->w;
+  if (!w->st_copy) CK(cudaStreamCreateWithFlags(&w->st_copy, cudaStreamNonBlocking));
+  cudaEvent_t ev = nullptr;
+  CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  if (n > 0) {
+    // the positions are converted in stream order; the copy to the host runs on the copy stream
+    // while the next steps run (they never touch the staging buffer)
+    float* stage = nullptr;
+    CK(cudaMallocAsync((void**)&stage, (size_t)n * 12, w->st));
+    launch_positions(h->pbuf[h->pcur], h->cap, off, n, h->dx, h->origin, stage, w->st);
+    CK(cudaEventRecord(ev, w->st));
+    CK(cudaStreamWaitEvent(w->st_copy, ev, 0));
+    CK(cudaMemcpyAsync(xyz, stage, (size_t)n * 12, cudaMemcpyDeviceToHost, w->st_copy));
+    CK(cudaFreeAsync(stage, w->st_copy));
+  }
+  CK(cudaEventRecord(ev, n > 0 ? w->st_copy : w->st));
+  *ticket = w->next_read++;
+  w->reads[*ticket] = ev;
+  return SI_OK;
+}
+
+int si_mpm_read_wait(si_mpm* h, uint64_t ticket) {
+  if (!h) return si_fail(SI_EINVAL, "null MPM handle");
+  cudaEvent_t ev = nullptr;
+  {
+    std::lock_guard<std::recursive_mutex> g(h->w->api_mu);
+    auto it = h->w->reads.find(ticket);
+    if (it == h->w->reads.end()) return si_fail(SI_EINVAL, "MPM: unknown read ticket");
+    ev = it->second;
+    h->w->reads.erase(it);
+  }
+  const cudaError_t e = cudaEventSynchronize(ev);   // outside the lock: other calls may proceed
+  cudaEventDestroy(ev);
+  return e == cudaSuccess ? SI_OK : si_fail(SI_EDEVICE, std::string("MPM: read failed: ") + cudaGetErrorString(e));
 }
 
 int si_mpm_set_colliders(si_mpm* h, const float* rows, int32_t k) {

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <thread>
@@ -64,6 +65,9 @@ struct si_world {
   double prof_ms[4] = {0, 0, 0, 0};
   cudaEvent_t pev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t marks[8] = {};
+  std::map<uint64_t, cudaEvent_t> reads;   // asynchronous readbacks in flight, by ticket
+  cudaStream_t st_copy = nullptr;          // their device-to-host copies, beside the next steps
+  uint64_t next_read = 1;
   int64_t launches = 0;             // kernels enqueued (graph replays add their kernel count)
 };
 

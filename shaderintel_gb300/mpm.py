@@ -431,6 +431,22 @@ class MPM:
             check(L.lib().si_mpm_read_positions(self._h, fptr(out), 0, n))
         return out
 
+    def readPositionsAsync(self, out=None):
+        """readPositions() as the reference's Promise: queues the copy behind the queued work and
+        returns a handle whose wait() gives the (count, 3) array. `out` (pinned memory keeps the
+        copy asynchronous) must stay alive until then."""
+        n = self.count
+        buf = np.empty((n, 3), np.float32) if out is None else out
+        t = ctypes.c_uint64()
+        check(L.lib().si_mpm_read_positions_async(self._h, fptr(buf), 0, n, ctypes.byref(t)))
+        sim = self
+
+        class _Read:
+            def wait(self):
+                check(L.lib().si_mpm_read_wait(sim._h, t.value))
+                return buf[:n]
+        return _Read()
+
     def readInstances(self, solidsOnly=False, size=1.0, matMask=None):
         """The sphere layer's instances as a headless buffer (spheres(), mpm.js:658-679): (count, 8)
         float32 — world xyz, radius (0 = culled by the material mask), world velocity, material id

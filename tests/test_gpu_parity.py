@@ -370,3 +370,27 @@ def test_sphere_layer_instances_headless():
     assert sim.fluidMask() == 1
     assert (solid[water, 3] == 0).all() and (solid[~water, 3] == radius).all()
     sim.destroy()
+
+
+def test_async_position_reads_match_sync_reads():
+    """readPositions() as a Promise: reads queued behind later steps give the same bytes as
+    synchronous reads taken at the same points."""
+    a = mixed_scene()
+    b = mixed_scene()
+    handles, want = [], []
+    for _ in range(3):
+        a.step()
+        handles.append(a.readPositionsAsync())
+        b.step()
+        want.append(b.readPositions())
+    for hnd, w in zip(handles, want):
+        assert np.array_equal(hnd.wait().view(np.uint32), w.view(np.uint32))
+    import ctypes
+    from shaderintel_gb300 import _lib as L
+    t = ctypes.c_uint64()
+    L.check(L.lib().si_mpm_read_positions_async(a._h, None, 0, 0, ctypes.byref(t)))
+    L.check(L.lib().si_mpm_read_wait(a._h, t.value))
+    with pytest.raises(SIError):                      # a ticket is waited on once
+        L.check(L.lib().si_mpm_read_wait(a._h, t.value))
+    a.destroy()
+    b.destroy()
