@@ -394,3 +394,17 @@ def test_async_position_reads_match_sync_reads():
         L.check(L.lib().si_mpm_read_wait(a._h, t.value))
     a.destroy()
     b.destroy()
+
+
+def test_large_grid_index_range():
+    """A 256^3 grid (16.8 M nodes, 67 M grid words) with particles in two far corners: node and word
+    indices near the top of the range, boxed grid updates far apart; bit-exact to the oracle."""
+    sim = MPM(grid=256, maxParticles=20000, substeps=4)
+    sim.add({"box": [[0.02, 0.02, 0.02], [0.05, 0.05, 0.05]]}, material="water", velocity=[1, 0, 0])
+    sim.add({"box": [[0.95, 0.9, 0.95], [0.98, 0.97, 0.98]]}, material="jelly", velocity=[0, -1, 0])
+    mats, cols, ncol, grav, vol4 = tables(sim)
+    rec = sim.readParticles()
+    sim.step(dt=sim.substepDt, K=6)
+    want, _, _ = O.substeps(rec, sim.dims, mats, cols, ncol, grav, vol4, 6, 0, 4, threads=8)
+    assert_records_equal(sim.readParticles(), want)
+    sim.destroy()
