@@ -100,6 +100,8 @@ SIGNATURES = {
                                    ctypes.POINTER(ctypes.c_int64)]),
     "si_mpm_read_positions_async": (ctypes.c_int, [vp, c_float_p, ctypes.c_int64, ctypes.c_int64, c_uint64_p]),
     "si_mpm_read_wait": (ctypes.c_int, [vp, ctypes.c_uint64]),
+    "si_mpm_device_ptr": (ctypes.c_int, [vp, ctypes.c_int32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_int64),
+                                         ctypes.POINTER(ctypes.c_int64)]),
     "si_mpm_read_instances": (ctypes.c_int, [vp, c_float_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_uint32,
                                              ctypes.c_double]),
     "si_mpm_couple": (ctypes.c_int, [vp, c_float_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_uint32,

@@ -1067,6 +1067,31 @@ int si_mpm_read_wait(si_mpm* h, uint64_t ticket) {
   return e == cudaSuccess ? SI_OK : si_fail(SI_EDEVICE, std::string("MPM: read failed: ") + cudaGetErrorString(e));
 }
 
+int si_mpm_device_ptr(si_mpm* h, int32_t what, const void** ptr, int64_t* count, int64_t* stride) {
+  GUARD(h);
+  if (!ptr || !count || !stride) return si_fail(SI_EINVAL, "null output");
+  if (what >= 0 && what < (int32_t)kStreams) {
+    *ptr = h->pbuf[h->pcur] + (size_t)what * (size_t)h->cap;
+    *count = h->count;
+    *stride = 16;
+  } else if (what == 8) {
+    *ptr = h->grid[h->gcur];
+    *count = h->nodes;
+    *stride = 16;
+  } else if (what == 9) {
+    *ptr = h->keys;
+    *count = h->count;
+    *stride = 4;
+  } else if (what == 10) {
+    *ptr = h->starts;
+    *count = (int64_t)h->num_blocks + 1;
+    *stride = 4;
+  } else {
+    return si_fail(SI_EINVAL, "si_mpm_device_ptr: what must be 0..10");
+  }
+  return SI_OK;
+}
+
 int si_mpm_set_colliders(si_mpm* h, const float* rows, int32_t k) {
   GUARD(h);
   if (k < 0 || (k && !rows)) return si_fail(SI_EINVAL, "MPM: bad collider table");

@@ -447,6 +447,11 @@ class MPM:
                 return buf[:n]
         return _Read()
 
+    def deviceView(self, which="P0"):
+        """Zero-copy read-only view of a device array: "P0".."P7" (the record's eight float4 streams),
+        "grid", "keys", "starts". Valid until the next step, sort, add or destroy."""
+        return DeviceView(self, which)
+
     def readInstances(self, solidsOnly=False, size=1.0, matMask=None):
         """The sphere layer's instances as a headless buffer (spheres(), mpm.js:658-679): (count, 8)
         float32 — world xyz, radius (0 = culled by the material mask), world velocity, material id
@@ -514,3 +519,21 @@ class MPM:
                 self._h = None
         except Exception:
             pass
+
+
+class DeviceView:
+    """A read-only device array of an MPM scene (si_mpm_device_ptr) with __cuda_array_interface__,
+    so torch.as_tensor(view, device="cuda") or another CUDA array library wraps it without a copy."""
+    _KINDS = {**{f"P{k}": (k, "<f4", 4) for k in range(8)}, "grid": (8, "<i4", 4), "keys": (9, "<u4", 1),
+              "starts": (10, "<u4", 1)}
+
+    def __init__(self, sim, which):
+        k, typestr, width = self._KINDS[which]
+        ptr, count, stride = ctypes.c_void_p(), ctypes.c_int64(), ctypes.c_int64()
+        check(L.lib().si_mpm_device_ptr(sim._h, k, ctypes.byref(ptr), ctypes.byref(count), ctypes.byref(stride)))
+        sim.sync()
+        shape = (count.value, width) if width > 1 else (count.value,)
+        # read-only by contract; the interface's read-only flag is left False because some consumers
+        # (torch) refuse it
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr.value or 0, False),
+                                         "version": 3, "strides": None}

@@ -408,3 +408,21 @@ def test_large_grid_index_range():
     want, _, _ = O.substeps(rec, sim.dims, mats, cols, ncol, grav, vol4, 6, 0, 4, threads=8)
     assert_records_equal(sim.readParticles(), want)
     sim.destroy()
+
+
+def test_device_views_wrap_without_copy():
+    """si_mpm_device_ptr: torch wraps the particle streams and the grid through
+    __cuda_array_interface__; the bytes equal the host reads."""
+    torch = pytest.importorskip("torch")
+    sim = mixed_scene()
+    sim.step()
+    P = sim.readParticles()
+    x = torch.as_tensor(sim.deviceView("P0"), device="cuda").cpu().numpy()
+    f2 = torch.as_tensor(sim.deviceView("P7"), device="cuda").cpu().numpy()
+    assert np.array_equal(x.view(np.uint32), P[:, 0:4].view(np.uint32))
+    assert np.array_equal(f2.view(np.uint32), P[:, 28:32].view(np.uint32))
+    g = torch.as_tensor(sim.deviceView("grid"), device="cuda").cpu().numpy()
+    assert np.array_equal(g, sim.readGrid())
+    keys = torch.as_tensor(sim.deviceView("keys"), device="cuda")
+    assert keys.shape[0] == sim.count
+    sim.destroy()
