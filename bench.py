@@ -489,6 +489,54 @@ def run_conservation(substeps=200):
             "energy_drift_rel": (s1["energy"] - s0["energy"]) / abs(s0["energy"]) if s0["energy"] else None}
 
 
+def run_extras():
+    """Costs of the added rows on the mixed 128^3 scene: add() sampled on the device against the host
+    sampler (wall time, same particles), and the coupling pass with 32 rigid bodies per substep."""
+    import numpy as np
+    from shaderintel_gb300 import MPM, World
+    from shaderintel_gb300.mpm import body_record
+    c = CONFIGS["mixed"]
+    g = c["grid"]
+    out = {}
+    for label, host in (("device", False), ("host", True)):
+        sim = MPM(None, grid=g, maxParticles=2300000, substeps=8)
+        sim.add({"box": [[0.4, 0.4, 0.4], [0.41, 0.41, 0.41]]}, material="water")   # warm the path
+        sim.clear()
+        sim.sync()
+        t = time.perf_counter()
+        for name, lo, hi, vel in c["blocks"]:
+            sim.add({"box": [[x / g for x in lo], [x / g for x in hi]]}, material=material_def(name), velocity=vel,
+                    _host=host)
+        sim.sync()
+        el = time.perf_counter() - t
+        out[f"add_{label}_ms"] = el * 1e3
+        out["add_particles"] = sim.count
+        sim.destroy()
+    rng = np.random.default_rng(3)
+    bodies = np.stack([body_record(rng.uniform(0.1, 0.9, 3), [rng.uniform(0.03, 0.08)] * 3,
+                                   "sphere" if k % 2 else "box", quaternion=rng.normal(size=4),
+                                   velocity=rng.uniform(-0.5, 0.5, 3), mass=1.0) for k in range(32)])
+    times = {}
+    for coupled in (False, True):
+        w = World()
+        sim = build_gpu("mixed", w)
+        if coupled:
+            sim.couple(bodies)
+        for _ in range(3):
+            sim.step()
+        w.mark(0)
+        for _ in range(10):
+            sim.step()
+        w.mark(1)
+        times[coupled] = w.elapsed(0, 1) / (10 * c["substeps"])
+        w.destroy()
+    out["couple_bodies"] = 32
+    out["substep_ms_uncoupled"] = times[False]
+    out["substep_ms_coupled"] = times[True]
+    out["couple_us_per_substep"] = (times[True] - times[False]) * 1e3
+    return out
+
+
 def traffic_per_launch(cfg):
     """DRAM bytes per k_g2p launch from the committed ncu summary, if one exists for this workload."""
     p = os.path.join(ROOT, "profiles", f"g2p_{cfg}_traffic.txt")
@@ -583,6 +631,7 @@ def main():
         out["served_saturated"] = run_served(sat, log)
     if world_size == 1:
         out["conservation"] = run_conservation()
+        out["extras"] = run_extras()
     if world_size > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
