@@ -231,6 +231,25 @@ __device__ __forceinline__ void scat_load(const float* sc, int chunk, int slot, 
   s.mass = sc[18 * chunk + slot];
 }
 
+// Visits every node of an ex x ey x ez tile once across the CTA and calls f(t, lx, ly, lz) with
+// t = lx + ex (ly + ey lz). The nodes are taken as columns along z: a thread splits its column
+// index into (lx, ly) once and then steps lz, instead of splitting every flat index with three
+// integer divisions by the runtime extents. When a layer holds fewer nodes than the CTA has
+// threads, floor(256 / layer) threads share each column at z offsets 0, 1, ...
+template <typename Fn>
+__device__ __forceinline__ void tile_walk(int ex, int ey, int ez, Fn&& f) {
+  const int tid = threadIdx.x;
+  const int exy = ex * ey;
+  const bool narrow = exy < kCtaThreads;
+  const int zs = narrow ? kCtaThreads / exy : 1;
+  const int z0 = narrow ? tid / exy : 0;
+  if (z0 >= zs) return;
+  for (int col = narrow ? tid - z0 * exy : tid; col < exy; col += narrow ? exy : kCtaThreads) {
+    const int ly = col / ex, lx = col - ly * ex;
+    for (int lz = z0; lz < ez; lz += zs) f(col + exy * lz, lx, ly, lz);
+  }
+}
+
 // CTA-wide P2G: AABB of the bases (mpm.js:353-377), tile if it fits (mpm.js:379-380), scatter,
 // flush of the non-zero tile nodes with global i32 atomics (mpm.js:385-399). The particles come from
 // `reg` (one per thread, valid if has_reg) when sc == nullptr, else from the `count` staged copies.
@@ -292,11 +311,10 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
   }
   if (use_tile) {
     cta_sync();
-    for (int t = tid; t < tnodes; t += blockDim.x) {
-      int m = tile[3 * tile_cap + t], mx = tile[t], my = tile[tile_cap + t], mz = tile[2 * tile_cap + t];
+    tile_walk(ex, ey, ez, [&](int t, int lx, int ly, int lz) {
+      const int m = tile[3 * tile_cap + t], mx = tile[t], my = tile[tile_cap + t], mz = tile[2 * tile_cap + t];
       if ((m | mx | my | mz) != 0) {
-        int lx = t % ex, ly = (t / ex) % ey, lz = t / (ex * ey);
-        int gx = o0 + lx, gy = o1 + ly, gz = o2 + lz;
+        const int gx = o0 + lx, gy = o1 + ly, gz = o2 + lz;
         if (in_grid(gx, gy, gz, dims)) {
           size_t gi = 4 * ((size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz));
           atomicAdd(&grid[gi], mx);
@@ -305,7 +323,7 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
           atomicAdd(&grid[gi + 3], m);
         }
       }
-    }
+    });
   }
   cta_sync();   // the tile and the staged inputs are reused by the next chunk
 }
@@ -720,14 +738,13 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
     const bool gtile = ex > 0 && gtn <= t.tile_nodes;
     // 2. stage the gather tile: vec4f(v, m) of every node under the stencils (zero outside the grid)
     if (gtile) {
-      for (int q = tid; q < (int)gtn; q += kCtaThreads) {
-        const int lx = q % ex, ly = (q / ex) % ey, lz = q / (ex * ey);
+      tile_walk(ex, ey, ez, [&](int q, int lx, int ly, int lz) {
         const int gx = o0 + lx, gy = o1 + ly, gz = o2 + lz;
         float4 n = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if ((unsigned)gx < (unsigned)dims[0] && (unsigned)gy < (unsigned)dims[1] && (unsigned)gz < (unsigned)dims[2])
           n = __ldg(&grid[(size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz)]);
         tilef[q] = n;
-      }
+      });
     }
     cta_sync();
     // 3. per-particle G2P
