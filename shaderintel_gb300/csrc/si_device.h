@@ -88,6 +88,7 @@ struct TickInfo {                // one tick's totals (kernel arguments)
   int32_t chunk;                 // particles per chunk (= kCtaThreads * ppt)
   int32_t tile_nodes;            // shared tile capacity in nodes
   uint32_t cchunks;              // 4^3 node tiles of the coupled scenes
+  float nz;                      // -0.0f: the addend of packed products (see mul2z in si_kernels.cu)
 };
 
 struct SortInfo {                // one tick's sort

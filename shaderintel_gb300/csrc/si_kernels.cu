@@ -18,6 +18,38 @@
 
 namespace si {
 
+// Packed FP32 pairs (FADD2 / FMUL2 / FFMA2 of sm_100+): each half rounds exactly like the scalar
+// add.rn / mul.rn / fma.rn. The scalar path relies on mul.rn and add.rn never being contracted; for
+// the packed forms ptxas does contract a mul.rn.f32x2 whose result feeds an add.rn.f32x2 into one
+// fma (measured: such a chain equals the fused chain bit for bit, in spite of .rn, a literal -0
+// addend or an empty asm barrier). So a product that feeds an add is formed by mul2z as
+// fma(x, y, nz) with nz = -0.0f read from the kernel arguments: the compiler cannot drop the
+// addend, an add of an fma result is not contracted, and x * y + (-0) rounds exactly like x * y
+// (including the sign of a zero product).
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 x, y, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n mul.rn.f32x2 r, x, y;\n"
+      " mov.b64 {%0, %1}, r;\n}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 x, y, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n add.rn.f32x2 r, x, y;\n"
+      " mov.b64 {%0, %1}, r;\n}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c);
+__device__ __forceinline__ float2 mul2z(float2 a, float2 b, float nz) { return fma2(a, b, make_float2(nz, nz)); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n .reg .b64 x, y, z, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n mov.b64 z, {%6, %7};\n"
+      " fma.rn.f32x2 r, x, y, z;\n mov.b64 {%0, %1}, r;\n}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
 // Shared tile: kTileNodes nodes, used first as the gather tile of the G2P (vec4f per node) and then
 // as the P2G scatter tile (four planes of i32, stride kTileNodes, so the four channel atomics of a
 // node share one address computation). TickInfo::tile_nodes (<= kTileNodes) is the usable capacity.
@@ -86,11 +118,12 @@ __device__ __forceinline__ bool in_grid(int gx, int gy, int gz, const int32_t* d
   return (unsigned)gx < (unsigned)d[0] && (unsigned)gy < (unsigned)d[1] && (unsigned)gz < (unsigned)d[2];
 }
 
-// i32(round(x * 2^22)) for |x| < 1 in two full-rate instructions: x * 2^22 is exact, so one fused
-// add of 1.5 * 2^23 rounds it to nearest-even exactly like rint, and the low bits of the sum are the
+// i32(round(x * 2^22)) for |x| < 1, a pair at a time: x * 2^22 is exact, so one fused add of
+// 1.5 * 2^23 rounds it to nearest-even exactly like rint, and the low bits of the sum are the
 // integer. Equal to to_fixed(x) wherever it is used (the caller proves |x| < 0.9 first).
-__device__ __forceinline__ int32_t to_fixed_small(float x) {
-  return __float_as_int(__fmaf_rn(x, 4194304.0f, 12582912.0f)) - 0x4B400000;
+__device__ __forceinline__ int2 to_fixed_small2(float2 x) {
+  const float2 f = fma2(x, make_float2(4194304.0f, 4194304.0f), make_float2(12582912.0f, 12582912.0f));
+  return make_int2(__float_as_int(f.x) - 0x4B400000, __float_as_int(f.y) - 0x4B400000);
 }
 
 // True when every value the particle scatters has |x| < 0.9: |wt| <= 1, |dpos| <= 1.5 and
@@ -116,7 +149,8 @@ __device__ __forceinline__ bool scatter_small(const Scat& s) {
 // in the unrotated order, so the i32 sums are unchanged.
 template <bool SMALL>
 __device__ __forceinline__ void scatter_impl(const Scat& s, const int32_t* dims, int* __restrict__ grid,
-                                             int* tile, int o0, int o1, int o2, int ex, int ey, bool use_tile) {
+                                             int* tile, int o0, int o1, int o2, int ex, int ey, bool use_tile,
+                                             float nz) {
   constexpr int tile_cap = kTileNodes;
   float wx[3], wy[3], wz[3];
   bspline(s.f[0], wx); bspline(s.f[1], wy); bspline(s.f[2], wz);
@@ -136,29 +170,47 @@ __device__ __forceinline__ void scatter_impl(const Scat& s, const int32_t* dims,
   }
   const int exy = ex * ey;
   const int t0 = ((s.b[2] - o2) * ey + (s.b[1] - o1)) * ex + (s.b[0] - o0);
+  // The x/y components of every product and sum go through one packed instruction, z and the mass
+  // scalar or paired with each other: the canonical expressions of mpm.js:333-347, per component
+  //   r = ((a0 dx + a3 dy) + a6 dz, ...),  m = wt (mv + r),  q = toFixed(m), toFixed(wt mass)
+  // with every product and sum rounded on its own.
+  const float2 aff01 = make_float2(s.aff[0], s.aff[1]), aff34 = make_float2(s.aff[3], s.aff[4]);
+  const float2 mv01 = make_float2(s.mv[0], s.mv[1]);
+  float2 p67[3];
+  float p8[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float dz = (float)c - s.f[2];
+    p67[c] = mul2z(make_float2(s.aff[6], s.aff[7]), make_float2(dz, dz), nz);
+    p8[c] = s.aff[8] * dz;
+  }
 #pragma unroll
   for (int ka = 0; ka < 3; ka++) {
     const int a = ia[ka];
     float dx = (float)a - s.f[0];
-    float ax0 = s.aff[0] * dx, ax1 = s.aff[1] * dx, ax2 = s.aff[2] * dx;
+    const float2 ax01 = mul2z(aff01, make_float2(dx, dx), nz);
+    const float ax2 = s.aff[2] * dx;
 #pragma unroll
     for (int kb = 0; kb < 3; kb++) {
       const int b = ib[kb];
       float dy = (float)b - s.f[1];
       float wab = wa[ka] * wb[kb];
-      float s0 = ax0 + s.aff[3] * dy, s1 = ax1 + s.aff[4] * dy, s2 = ax2 + s.aff[5] * dy;
+      const float2 s01 = add2(ax01, mul2z(aff34, make_float2(dy, dy), nz));
+      const float s2 = ax2 + s.aff[5] * dy;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        float dz = (float)c - s.f[2];
         float wt = wab * wz[c];
-        float r0 = s0 + s.aff[6] * dz, r1 = s1 + s.aff[7] * dz, r2 = s2 + s.aff[8] * dz;
-        const float m0 = wt * (s.mv[0] + r0), m1 = wt * (s.mv[1] + r1), m2 = wt * (s.mv[2] + r2);
-        const float m3v = wt * s.mass;
         int32_t q0, q1, q2, q3;
+        const float2 r01 = add2(s01, p67[c]);
+        const float r2 = s2 + p8[c];
+        const float2 ww = make_float2(wt, wt);   // products that feed no add: plain mul2
+        const float2 m01 = mul2(ww, add2(mv01, r01));
+        const float2 m23 = mul2(ww, make_float2(s.mv[2] + r2, s.mass));
         if (SMALL) {
-          q0 = to_fixed_small(m0); q1 = to_fixed_small(m1); q2 = to_fixed_small(m2); q3 = to_fixed_small(m3v);
+          const int2 q01 = to_fixed_small2(m01), q23 = to_fixed_small2(m23);
+          q0 = q01.x; q1 = q01.y; q2 = q23.x; q3 = q23.y;
         } else {
-          q0 = to_fixed(m0); q1 = to_fixed(m1); q2 = to_fixed(m2); q3 = to_fixed(m3v);
+          q0 = to_fixed(m01.x); q1 = to_fixed(m01.y); q2 = to_fixed(m23.x); q3 = to_fixed(m23.y);
         }
         if (use_tile) {
           const int ti = t0 + a + ex * b + exy * c;
@@ -184,9 +236,10 @@ __device__ __forceinline__ void scatter_impl(const Scat& s, const int32_t* dims,
 // Every lane of the warp calls this (idle lanes with a silenced copy); the fast conversion is chosen
 // per warp so the lanes stay on one path.
 __device__ __forceinline__ void scatter_one(const Scat& s, const int32_t* dims, int* __restrict__ grid,
-                                            int* tile, int o0, int o1, int o2, int ex, int ey, bool use_tile) {
-  if (__all_sync(0xffffffffu, scatter_small(s))) scatter_impl<true>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
-  else scatter_impl<false>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
+                                            int* tile, int o0, int o1, int o2, int ex, int ey, bool use_tile,
+                                            float nz) {
+  if (__all_sync(0xffffffffu, scatter_small(s))) scatter_impl<true>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile, nz);
+  else scatter_impl<false>(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile, nz);
 }
 
 // P2G inputs of the CTA's particles, staged in shared memory (SoA, kScatWords words per particle)
@@ -255,7 +308,7 @@ __device__ __forceinline__ void tile_walk(int ex, int ey, int ez, Fn&& f) {
 // `reg` (one per thread, valid if has_reg) when sc == nullptr, else from the `count` staged copies.
 __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const float* sc, int chunk, int count,
                                             const int32_t* dims, int* __restrict__ grid, bool force_global,
-                                            int tile_nodes, int* tile, int* sbox, int32_t* scene_box) {
+                                            int tile_nodes, int* tile, int* sbox, int32_t* scene_box, float nz) {
   constexpr int tile_cap = kTileNodes;
   const int tid = threadIdx.x;
   if (tid < 3) { sbox[tid] = 0x3fffffff; sbox[3 + tid] = -0x3fffffff; }
@@ -300,13 +353,13 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
     cta_sync();
   }
   if (sc == nullptr) {
-    scatter_one(reg, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);   // every lane (has_reg is true)
+    scatter_one(reg, dims, grid, tile, o0, o1, o2, ex, ey, use_tile, nz);   // every lane (has_reg is true)
   } else {
 #pragma unroll 1
     for (int slot = tid; slot < count; slot += blockDim.x) {
       Scat s;
       scat_load(sc, chunk, slot, s);
-      scatter_one(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile);
+      scatter_one(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile, nz);
     }
   }
   if (use_tile) {
@@ -360,7 +413,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t
     }
     cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
                 reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox,
-                ts.box_cur);
+                ts.box_cur, t.nz);
   }
 }
 
@@ -518,15 +571,18 @@ template <bool TILE>
 __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, float4& C1, float4& C2,
                                              float4& F0, float4& F1, float4& F2, const SceneParams* prm,
                                              const float4* __restrict__ grid, const float4* tilef, int o0,
-                                             int o1, int o2, int sx, int sxy) {
+                                             int o1, int o2, int sx, int sxy, float negz) {
   const int32_t dx0 = prm->dims[0], dx1 = prm->dims[1], dx2 = prm->dims[2];
   const int b0 = base_of(X.x, dx0), b1 = base_of(X.y, dx1), b2 = base_of(X.z, dx2);
   const float f0 = X.x - (float)b0, f1 = X.y - (float)b1, f2 = X.z - (float)b2;
   float wx[3], wy[3], wz[3];
   bspline(f0, wx); bspline(f1, wy); bspline(f2, wz);
-  v3 v = V(0.0f, 0.0f, 0.0f);
+  v3 v;
   m3 B;
-  B.c[0] = V(0.0f, 0.0f, 0.0f); B.c[1] = V(0.0f, 0.0f, 0.0f); B.c[2] = V(0.0f, 0.0f, 0.0f);
+  // v += t and B += outer3(t, dpos) with t = wt gv (mpm.js:500-509), product and sum rounded
+  // separately, in packed accumulators: (v.x, v.y), (B0.x, B0.y), (B1.x, B1.y), (B2.x, B2.y),
+  // (B0.z, B1.z), (v.z, B2.z), where column k of B gains t dpos_k.
+  float2 vxy = make_float2(0.0f, 0.0f), bxy0 = vxy, bxy1 = vxy, bxy2 = vxy, z01 = vxy, z2v = vxy;
   const int t0 = TILE ? ((b2 - o2) * (sxy / sx) + (b1 - o1)) * sx + (b0 - o0) : 0;
 #pragma unroll 1
   for (int a = 0; a < 3; a++) {
@@ -552,15 +608,22 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
             gv = V(n.x, n.y, n.z);
           }
         }
-        const v3 t = vscale(wt, gv);
-        v = vadd(v, t);
-        // B += outer3(t, dpos): column k gains t * dpos_k, product and sum rounded separately
-        B.c[0] = V(B.c[0].x + t.x * dpx, B.c[0].y + t.y * dpx, B.c[0].z + t.z * dpx);
-        B.c[1] = V(B.c[1].x + t.x * dpy, B.c[1].y + t.y * dpy, B.c[1].z + t.z * dpy);
-        B.c[2] = V(B.c[2].x + t.x * dpz, B.c[2].y + t.y * dpz, B.c[2].z + t.z * dpz);
+        const float2 txy = mul2z(make_float2(wt, wt), make_float2(gv.x, gv.y), negz);
+        const float tz = wt * gv.z;
+        const float2 tzz = make_float2(tz, tz);
+        vxy = add2(vxy, txy);
+        bxy0 = add2(bxy0, mul2z(txy, make_float2(dpx, dpx), negz));
+        bxy1 = add2(bxy1, mul2z(txy, make_float2(dpy, dpy), negz));
+        bxy2 = add2(bxy2, mul2z(txy, make_float2(dpz, dpz), negz));
+        z01 = add2(z01, mul2z(tzz, make_float2(dpx, dpy), negz));
+        z2v = add2(z2v, mul2z(tzz, make_float2(1.0f, dpz), negz));   // (t.z, t.z dpz): t.z * 1 is exact
       }
     }
   }
+  v = V(vxy.x, vxy.y, z2v.x);
+  B.c[0] = V(bxy0.x, bxy0.y, z01.x);
+  B.c[1] = V(bxy1.x, bxy1.y, z01.y);
+  B.c[2] = V(bxy2.x, bxy2.y, z2v.y);
   m3 C;
   C.c[0] = vscale(4.0f, B.c[0]); C.c[1] = vscale(4.0f, B.c[1]); C.c[2] = vscale(4.0f, B.c[2]);
   const float sp = vlen(v);
@@ -760,8 +823,8 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
       float4 v = make_float4(0.0f, 0.0f, 0.0f, __ldcs(reinterpret_cast<const float*>(&Pin[cap + j]) + 3));
       float4 c0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c1 = c0, c2 = c0;
       float4 f0 = __ldcs(&Pin[5 * cap + j]), f1 = __ldcs(&Pin[6 * cap + j]), f2 = __ldcs(&Pin[7 * cap + j]);
-      if (gtile) g2p_particle<true>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, o0, o1, o2, ex, ex * ey);
-      else g2p_particle<false>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, 0, 0, 0, 1, 1);
+      if (gtile) g2p_particle<true>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, o0, o1, o2, ex, ex * ey, t.nz);
+      else g2p_particle<false>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, 0, 0, 0, 1, 1, t.nz);
       if (valid) {
         __stcs(&P[i], x); __stcs(&P[cap + i], v); __stcs(&P[2 * cap + i], c0); __stcs(&P[3 * cap + i], c1);
         __stcs(&P[4 * cap + i], c2); __stcs(&P[5 * cap + i], f0); __stcs(&P[6 * cap + i], f1);
@@ -778,7 +841,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
     if (fuse)
       cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
                   reinterpret_cast<int*>(ts.grid_next), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox,
-                  ts.box_next);
+                  ts.box_next, t.nz);
     else
       cta_sync();
   }

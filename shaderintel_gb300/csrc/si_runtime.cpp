@@ -336,6 +336,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   t.cchunks = k.cchunks;
   t.chunk = kCtaThreads * w->ppt;
   t.tile_nodes = w->tile_nodes;
+  t.nz = -0.0f;
   cudaStream_t st = w->st;
   if (profile) cudaEventRecord(w->pev[0], st);
   const uint32_t* perm = nullptr;
