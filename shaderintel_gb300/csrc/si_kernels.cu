@@ -818,11 +818,15 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
       const int slot = min(k * kCtaThreads + tid, count - 1);
       const int64_t i = first + slot, j = js[k];
       // G2P reads x, J (v.w) and F; v.xyz, C and the stress are recomputed (mpm.js:479-559), so their
-      // 52 bytes per particle are not loaded
+      // 52 bytes per particle are not loaded. A fluid's F is reset to I (mpm.js:520-525) and its input
+      // F is never read, so its 48 bytes are loaded only for the other models.
       float4 x = xs[k];
       float4 v = make_float4(0.0f, 0.0f, 0.0f, __ldcs(reinterpret_cast<const float*>(&Pin[cap + j]) + 3));
       float4 c0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c1 = c0, c2 = c0;
-      float4 f0 = __ldcs(&Pin[5 * cap + j]), f1 = __ldcs(&Pin[6 * cap + j]), f2 = __ldcs(&Pin[7 * cap + j]);
+      float4 f0 = c0, f1 = c0, f2 = c0;
+      if (__float_as_uint(__ldg(&prm->mats[(__float_as_uint(x.w) & 7u) * 3].x)) != 0u) {
+        f0 = __ldcs(&Pin[5 * cap + j]); f1 = __ldcs(&Pin[6 * cap + j]); f2 = __ldcs(&Pin[7 * cap + j]);
+      }
       if (gtile) g2p_particle<true>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, o0, o1, o2, ex, ex * ey, t.nz);
       else g2p_particle<false>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, 0, 0, 0, 1, 1, t.nz);
       if (valid) {
