@@ -18,38 +18,6 @@
 
 namespace si {
 
-// Packed FP32 pairs (FADD2 / FMUL2 / FFMA2 of sm_100+): each half rounds exactly like the scalar
-// add.rn / mul.rn / fma.rn. The scalar path relies on mul.rn and add.rn never being contracted; for
-// the packed forms ptxas does contract a mul.rn.f32x2 whose result feeds an add.rn.f32x2 into one
-// fma (measured: such a chain equals the fused chain bit for bit, in spite of .rn, a literal -0
-// addend or an empty asm barrier). So a product that feeds an add is formed by mul2z as
-// fma(x, y, nz) with nz = -0.0f read from the kernel arguments: the compiler cannot drop the
-// addend, an add of an fma result is not contracted, and x * y + (-0) rounds exactly like x * y
-// (including the sign of a zero product).
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-  float2 d;
-  asm("{\n .reg .b64 x, y, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n mul.rn.f32x2 r, x, y;\n"
-      " mov.b64 {%0, %1}, r;\n}"
-      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return d;
-}
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-  float2 d;
-  asm("{\n .reg .b64 x, y, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n add.rn.f32x2 r, x, y;\n"
-      " mov.b64 {%0, %1}, r;\n}"
-      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return d;
-}
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c);
-__device__ __forceinline__ float2 mul2z(float2 a, float2 b, float nz) { return fma2(a, b, make_float2(nz, nz)); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-  float2 d;
-  asm("{\n .reg .b64 x, y, z, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n mov.b64 z, {%6, %7};\n"
-      " fma.rn.f32x2 r, x, y, z;\n mov.b64 {%0, %1}, r;\n}"
-      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-  return d;
-}
-
 // Shared tile: kTileNodes nodes, used first as the gather tile of the G2P (vec4f per node) and then
 // as the P2G scatter tile (four planes of i32, stride kTileNodes, so the four channel atomics of a
 // node share one address computation). TickInfo::tile_nodes (<= kTileNodes) is the usable capacity.

@@ -12,6 +12,37 @@ namespace si {
 struct v3 { float x, y, z; };
 struct m3 { v3 c[3]; };   // columns
 
+// Packed FP32 pairs (FADD2 / FMUL2 / FFMA2 of sm_100+): each half rounds exactly like the scalar
+// add.rn / mul.rn / fma.rn. The scalar path relies on mul.rn and add.rn never being contracted; for
+// the packed forms ptxas does contract a mul.rn.f32x2 whose result feeds an add.rn.f32x2 into one
+// fma (measured: such a chain equals the fused chain bit for bit, in spite of .rn, a literal -0
+// addend or an empty asm barrier). So a product that feeds an add is formed by mul2z as
+// fma(x, y, nz) with nz = -0.0f read from the kernel arguments: the compiler cannot drop the
+// addend, an add of an fma result is not contracted, and x * y + (-0) rounds exactly like x * y
+// (including the sign of a zero product).
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 x, y, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n mul.rn.f32x2 r, x, y;\n"
+      " mov.b64 {%0, %1}, r;\n}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 x, y, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n add.rn.f32x2 r, x, y;\n"
+      " mov.b64 {%0, %1}, r;\n}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n .reg .b64 x, y, z, r;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n mov.b64 z, {%6, %7};\n"
+      " fma.rn.f32x2 r, x, y, z;\n mov.b64 {%0, %1}, r;\n}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+__device__ __forceinline__ float2 mul2z(float2 a, float2 b, float nz) { return fma2(a, b, make_float2(nz, nz)); }
+
 __device__ __forceinline__ v3 V(float x, float y, float z) { v3 r; r.x = x; r.y = y; r.z = z; return r; }
 __device__ __forceinline__ v3 vadd(v3 a, v3 b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ __forceinline__ v3 vsub(v3 a, v3 b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
@@ -137,33 +168,36 @@ __device__ __forceinline__ float si_expf(float x) {
 __device__ __forceinline__ float get(const v3& v, int r) { return r == 0 ? v.x : (r == 1 ? v.y : v.z); }
 __device__ __forceinline__ void put(v3& v, int r, float x) { if (r == 0) v.x = x; else if (r == 1) v.y = x; else v.z = x; }
 
+// sg / y with sg = +-1 is +-(1 / y) exactly, and 1 / y is the correctly rounded reciprocal
+// (__frcp_rn), cheaper than a general IEEE division. (Packing the rotation updates into FP32 pairs
+// was bit-exact too but raised the kernel's spills and cost more on the scenes without SVD.)
 template <int p, int q>
 __device__ __forceinline__ void jacobi_rotate(m3& A, m3& Vm) {
   float apq = get(A.c[q], p);
   if (fabsf(apq) < 1e-30f) return;
   float theta = (get(A.c[q], q) - get(A.c[p], p)) / (2.0f * apq);
   float sg = theta >= 0.0f ? 1.0f : -1.0f;
-  float t = sg / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
-  float c = 1.0f / sqrtf(t * t + 1.0f);
+  float t = sg * __frcp_rn(fabsf(theta) + sqrtf(theta * theta + 1.0f));
+  float c = __frcp_rn(sqrtf(t * t + 1.0f));
   float s = t * c;
   float ns = -s;
   // T = J^T A: rows p and q of every column
 #pragma unroll
   for (int j = 0; j < 3; j++) {
-    float ap = get(A.c[j], p), aq = get(A.c[j], q);
+    const float ap = get(A.c[j], p), aq = get(A.c[j], q);
     put(A.c[j], p, c * ap + ns * aq);
     put(A.c[j], q, s * ap + c * aq);
   }
   // A' = T J: columns p and q
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    float tp = get(A.c[p], i), tq = get(A.c[q], i);
+    const float tp = get(A.c[p], i), tq = get(A.c[q], i);
     put(A.c[p], i, tp * c + tq * ns);
     put(A.c[q], i, tp * s + tq * c);
   }
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    float vp = get(Vm.c[p], i), vq = get(Vm.c[q], i);
+    const float vp = get(Vm.c[p], i), vq = get(Vm.c[q], i);
     put(Vm.c[p], i, vp * c + vq * ns);
     put(Vm.c[q], i, vp * s + vq * c);
   }
