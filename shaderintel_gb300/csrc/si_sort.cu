@@ -3,9 +3,10 @@
 // The reference counts keys with global atomics, so the order inside a block depends on atomic
 // timing. Here the particles of every sorting scene are concatenated with key = bin_base + block key
 // and sorted by a stable LSD radix sort (8-bit digits; per pass: tile histograms, a scan per digit,
-// a stable scatter ranked with warp match + shared-memory prefixes). It is deterministic, has no
-// waits between CTAs, and yields the reference's counts and starts exactly; each scene's particles
-// stay inside its own segment because the bin ranges are ordered like the segments.
+// a stable scatter in which each warp ranks a contiguous segment of its tile with warp match and
+// per-warp digit counters). It is deterministic, has no waits between CTAs, and yields the
+// reference's counts and starts exactly; each scene's particles stay inside its own segment because
+// the bin ranges are ordered like the segments.
 #include <algorithm>
 #include <mutex>
 
@@ -53,10 +54,15 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_hist(const uint32_t* __re
     h[threadIdx.x] = 0;
     cta_sync();
     const uint32_t base = tile * kSortTile;
+    // the keys arrive nearly sorted, so most lanes of a warp share a digit: one add per distinct
+    // digit of the warp (its lowest lane adds the group's size) instead of one per lane
+    const unsigned lane = threadIdx.x & 31u;
 #pragma unroll
     for (int r = 0; r < kItems; r++) {
-      uint32_t e = base + r * kCtaThreads + threadIdx.x;
-      if (e < n) atomicAdd(&h[(__ldg(&keys[e]) >> shift) & 255u], 1u);
+      const uint32_t e = base + r * kCtaThreads + threadIdx.x;
+      const uint32_t d = e < n ? (__ldg(&keys[e]) >> shift) & 255u : 256u;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      if (d < 256u && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
     }
     cta_sync();
     hist[threadIdx.x * tiles + tile] = h[threadIdx.x];
@@ -94,14 +100,20 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
   if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
 }
 
+// Stable scatter of one pass. Warp w of a tile owns the kSortTile / kWarps consecutive keys from
+// tile * kSortTile + w * kSeg; it counts their digits (one add per distinct digit and round, by the
+// group's lowest lane), a per-digit prefix over the warps turns the counts into each warp's first
+// position, and a second walk over the same keys stores each at that position plus its rank among
+// the earlier lanes of its round with the same digit. The rank order is (warp, round, lane), which is
+// the keys' order in the tile, so equal digits keep their input order.
 __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                               uint32_t* kout, uint32_t* vout, uint32_t n, int shift,
                                                               const uint32_t* __restrict__ hist, const uint32_t* __restrict__ digit_total,
                                                               uint32_t tiles) {
+  constexpr int kSeg = kSortTile / kWarps;   // 512 keys per warp, kItems rounds of 32
+  static_assert(kSeg == kItems * 32, "a warp's segment is kItems rounds of 32 keys");
   __shared__ uint32_t dbase[256];
-  __shared__ uint32_t wcount[kWarps][256];
-  __shared__ uint32_t wpre[kWarps][256];
-  __shared__ uint32_t run[256];
+  __shared__ uint32_t woff[kWarps][256];
   __shared__ uint32_t wsum[kWarps];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // exclusive scan of the digit totals (same in every CTA)
@@ -118,41 +130,54 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* _
     for (int w = 0; w < warp; w++) pre += wsum[w];
     dbase[tid] = pre + x - v;
   }
-  for (int w = 0; w < kWarps; w++) wcount[w][tid] = 0;
-  cta_sync();
   const unsigned lt_mask = (1u << lane) - 1u;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    run[tid] = dbase[tid] + hist[tid * tiles + tile];
+    for (int w = 0; w < kWarps; w++) woff[w][tid] = 0;
     cta_sync();
-    const uint32_t base = tile * kSortTile;
-    for (int r = 0; r < kItems; r++) {
-      const uint32_t e = base + r * kCtaThreads + tid;
-      const bool ok = e < n;
-      uint32_t key = 0, val = 0, d = 256;
-      if (ok) { key = kin[e]; val = vin[e]; d = (key >> shift) & 255u; }
-      const unsigned peers = __match_any_sync(0xffffffffu, d);
-      const unsigned rank = __popc(peers & lt_mask);
-      if (ok && rank == 0) wcount[warp][d] = __popc(peers);
-      cta_sync();
-      {
-        uint32_t acc = run[tid];
+    const uint32_t wbase = tile * kSortTile + (uint32_t)warp * kSeg;
+    uint32_t key[kItems], val[kItems];
+    // 1. the warp's digit counts
 #pragma unroll
-        for (int w = 0; w < kWarps; w++) {
-          uint32_t c = wcount[w][tid];
-          wpre[w][tid] = acc;
-          acc += c;
-          wcount[w][tid] = 0;
-        }
-        run[tid] = acc;
-      }
-      cta_sync();
-      if (ok) {
-        const uint32_t pos = wpre[warp][d] + rank;
-        kout[pos] = key;
-        vout[pos] = val;
-      }
-      cta_sync();
+    for (int r = 0; r < kItems; r++) {
+      const uint32_t e = wbase + r * 32 + lane;
+      const bool ok = e < n;
+      key[r] = ok ? kin[e] : 0u;
+      val[r] = ok ? vin[e] : 0u;
+      const uint32_t d = ok ? (key[r] >> shift) & 255u : 256u;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      if (ok && (peers & lt_mask) == 0u) woff[warp][d] += (uint32_t)__popc(peers);
+      __syncwarp();
     }
+    cta_sync();
+    // 2. per digit: the first position of each warp's keys (tile base of the digit from the scan)
+    {
+      uint32_t acc = dbase[tid] + hist[tid * tiles + tile];
+#pragma unroll
+      for (int w = 0; w < kWarps; w++) {
+        const uint32_t c = woff[w][tid];
+        woff[w][tid] = acc;
+        acc += c;
+      }
+    }
+    cta_sync();
+    // 3. ranks and stores, in the same order as the counts
+#pragma unroll
+    for (int r = 0; r < kItems; r++) {
+      const uint32_t e = wbase + r * 32 + lane;
+      const bool ok = e < n;
+      const uint32_t d = ok ? (key[r] >> shift) & 255u : 256u;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t rank = (uint32_t)__popc(peers & lt_mask);
+      const uint32_t at = ok ? woff[warp][d] : 0u;
+      __syncwarp();
+      if (ok) {
+        kout[at + rank] = key[r];
+        vout[at + rank] = val[r];
+        if (rank == 0) woff[warp][d] = at + (uint32_t)__popc(peers);
+      }
+      __syncwarp();
+    }
+    cta_sync();   // woff is cleared for the next tile
   }
 }
 
