@@ -172,11 +172,46 @@ static void build_params(const si_mpm* h, SceneParams* p) {
   p->band = (float)h->band;
 }
 
+// The event guarding a staging slot: wait for the copy that last used it, or create it.
+static int stage_slot_ready(cudaEvent_t& ev) {
+  if (ev) CK(cudaEventSynchronize(ev));
+  else CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  return SI_OK;
+}
+
+// Host-to-device copy through a pinned staging buffer of the world (see si_world::stage).
+static int stage_upload(si_world* w, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return SI_OK;
+  const int slot = w->stage_next;
+  w->stage_next = (slot + 1) % si_world::kStageSlots;
+  int r = stage_slot_ready(w->stage_ev[slot]);
+  if (r) return r;
+  if (w->stage_cap[slot] < bytes) {
+    if (w->stage[slot]) CK(cudaFreeHost(w->stage[slot]));
+    w->stage[slot] = nullptr;
+    w->stage_cap[slot] = 0;
+    const size_t cap = std::max<size_t>(std::max<size_t>(bytes, 4096), 2 * w->stage_cap[slot]);
+    CK(cudaHostAlloc(&w->stage[slot], cap, cudaHostAllocDefault));
+    w->stage_cap[slot] = cap;
+  }
+  std::memcpy(w->stage[slot], src, bytes);
+  CK(cudaMemcpyAsync(dst, w->stage[slot], bytes, cudaMemcpyHostToDevice, w->st));
+  CK(cudaEventRecord(w->stage_ev[slot], w->st));
+  return SI_OK;
+}
+
 static int upload_params(si_mpm* h) {
   if (!h->prm_dirty) return SI_OK;
-  SceneParams p;
-  build_params(h, &p);
-  CK(cudaMemcpyAsync(h->prm, &p, sizeof(p), cudaMemcpyHostToDevice, h->w->st));
+  si_world* w = h->w;
+  if (!w->prm_ring) CK(cudaHostAlloc((void**)&w->prm_ring, sizeof(SceneParams) * si_world::kPrmSlots, cudaHostAllocDefault));
+  const int slot = w->prm_next;
+  w->prm_next = (slot + 1) % si_world::kPrmSlots;
+  int r = stage_slot_ready(w->prm_ev[slot]);
+  if (r) return r;
+  SceneParams* p = w->prm_ring + slot;
+  build_params(h, p);
+  CK(cudaMemcpyAsync(h->prm, p, sizeof(*p), cudaMemcpyHostToDevice, w->st));
+  CK(cudaEventRecord(w->prm_ev[slot], w->st));
   h->prm_dirty = false;
   return SI_OK;
 }
@@ -432,7 +467,8 @@ static int run_plan(si_world* w, std::vector<HostTick>& plan) {
   if (graph_ok) {
     auto g = std::make_unique<GraphPlan>();
     CK(cudaMalloc((void**)&g->table, std::max<size_t>(bytes.size(), 16)));
-    CK(cudaMemcpyAsync(g->table, bytes.data(), bytes.size(), cudaMemcpyHostToDevice, w->st));
+    r = stage_upload(w, g->table, bytes.data(), bytes.size());
+    if (r) return r;
     CK(cudaStreamBeginCapture(w->st, cudaStreamCaptureModeThreadLocal));
     size_t off = 0;
     for (const HostTick& k : plan) {
@@ -476,7 +512,8 @@ static int run_plan(si_world* w, std::vector<HostTick>& plan) {
   if (r) return r;
   w->tab = (TickScene*)tab;
   w->tab_cap = cap;
-  CK(cudaMemcpyAsync(w->tab, bytes.data(), bytes.size(), cudaMemcpyHostToDevice, w->st));
+  r = stage_upload(w, w->tab, bytes.data(), bytes.size());
+  if (r) return r;
   size_t off = 0;
   for (const HostTick& k : plan) {
     enqueue_tick(w, k, reinterpret_cast<const TickScene*>(reinterpret_cast<uint8_t*>(w->tab) + off), w->profile);
@@ -615,6 +652,12 @@ int si_world_destroy(si_world* w) {
   }
   for (auto& kv : w->reads) cudaEventDestroy(kv.second);
   w->reads.clear();
+  for (auto& e : w->prm_ev) if (e) cudaEventDestroy(e);
+  for (auto& e : w->stage_ev) if (e) cudaEventDestroy(e);
+  if (w->prm_ring) cudaFreeHost(w->prm_ring);
+  w->prm_ring = nullptr;
+  for (int i = 0; i < si_world::kStageSlots; i++)
+    if (w->stage[i]) { cudaFreeHost(w->stage[i]); w->stage[i] = nullptr; }
   cudaStreamDestroy(w->st);
   w->destroyed = true;
   return SI_OK;
@@ -1133,9 +1176,7 @@ int si_mpm_set_bodies(si_mpm* h, const float* bodies, int32_t n) {
   GUARD(h);
   if (!bodies || n != h->nbodies) return si_fail(SI_EINVAL, "MPM: the body table must keep the coupled count");
   if (n == 0) return SI_OK;
-  CK(cudaMemcpyAsync(h->bodies, bodies, (size_t)n * 192, cudaMemcpyHostToDevice, h->w->st));
-  CK(cudaStreamSynchronize(h->w->st));
-  return SI_OK;
+  return stage_upload(h->w, h->bodies, bodies, (size_t)n * 192);   // the caller's table is free on return
 }
 
 int si_mpm_read_impulses(si_mpm* h, float* out, int32_t n) {

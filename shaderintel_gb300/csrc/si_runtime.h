@@ -69,6 +69,19 @@ struct si_world {
   cudaStream_t st_copy = nullptr;          // their device-to-host copies, beside the next steps
   uint64_t next_read = 1;
   int64_t launches = 0;             // kernels enqueued (graph replays add their kernel count)
+  // Pinned staging of host-to-device uploads. From pageable memory cudaMemcpyAsync first waits for
+  // the stream, so a per-frame parameter or table upload would hold the host until the GPU drained
+  // and leave the GPU idle while the next frame is enqueued. A slot is reused once the copy out of
+  // it has run (its event), which only waits when the host is a whole ring ahead of the stream.
+  static constexpr int kPrmSlots = 1024;
+  si::SceneParams* prm_ring = nullptr;      // kPrmSlots slots, allocated on first use
+  cudaEvent_t prm_ev[kPrmSlots] = {};
+  int prm_next = 0;
+  static constexpr int kStageSlots = 8;
+  void* stage[kStageSlots] = {};            // tick tables and body tables, grown on demand
+  size_t stage_cap[kStageSlots] = {};
+  cudaEvent_t stage_ev[kStageSlots] = {};
+  int stage_next = 0;
 };
 
 struct si_mpm {
