@@ -254,6 +254,26 @@ def test_step_in_pieces_equals_one_call():
     b.destroy()
 
 
+def test_collider_moving_every_frame_bit_exact():
+    """A sphere collider that moves every frame: its table goes to the device before each step through
+    the world's pinned staging slots (1,100 uploads, more than the 1,024 slots, so slots are reused
+    while earlier frames may still be queued); the trajectory equals the oracle stepped frame by frame
+    with the same tables."""
+    sim = MPM(grid=16, maxParticles=4000, substeps=1)
+    sim.add({"box": [[0.25, 0.2, 0.25], [0.6, 0.7, 0.6]]}, material="water", seed=2)
+    P, sc = sim.readParticles(), 0
+    for f in range(1100):
+        x = 0.25 + 0.5 * (f % 200) / 200
+        sim.setColliders([{"type": "sphere", "center": [x, 0.3, 0.45], "radius": 0.09, "velocity": [0.5, 0, 0],
+                           "friction": 0.3}])
+        sim.step()
+        mats, cols, ncol, grav, vol4 = tables(sim)
+        P, _, sc = O.substeps(P, sim.dims, mats, cols, ncol, grav, vol4, 1, sc)
+    assert sim.stepCount == sc == 1100
+    assert_records_equal(sim.readParticles(), P)
+    sim.destroy()
+
+
 def test_dam_break_reference():
     """tests/physics.test.js:43-59: 48^3, water + jelly, 150 frames."""
     sim = MPM(grid=48, maxParticles=200000, substeps=8)
