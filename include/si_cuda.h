@@ -140,7 +140,9 @@ int si_mpm_read_positions(si_mpm* h, float* xyz, int64_t offset, int64_t n);
 int si_mpm_read_positions_async(si_mpm* h, float* xyz, int64_t offset, int64_t n, uint64_t* ticket);
 int si_mpm_read_wait(si_mpm* h, uint64_t ticket);
 /* colBuf.writeOrdered of _uploadColliders, mpm.js:276-293: k <= 16 rows of 12 floats in lattice
- * units [kind(u32), center xyz, radius | half xyz | normal xyz, friction, velocity xyz (cells/substep), 0]. */
+ * units [kind(u32), center xyz, radius | half xyz | normal xyz, friction, velocity xyz (cells/substep), 0].
+ * Taken by value; it reaches the device with the next step's parameters, ordered after the work
+ * already queued, without waiting for it. */
 int si_mpm_set_colliders(si_mpm* h, const float* rows, int32_t k);
 /* gravity setter (m/s^2); applied as g*dt^2/dx per substep (mpm.js:588). */
 int si_mpm_set_gravity(si_mpm* h, const double g[3]);
@@ -229,7 +231,9 @@ int si_mpm_emit(si_mpm* h, int32_t shape, const double a[3], const double b[3], 
  * density_scale 1 are the reference's defaults. */
 int si_mpm_couple(si_mpm* h, const float* bodies, int32_t n, double friction, double band, uint32_t mask,
                   double density_scale);
-/* The rigid world moved: new body records (same count) for the next substeps (the B buffer). */
+/* The rigid world moved: new body records (same count) for the next substeps (the B buffer). The
+ * table is copied before the call returns (into pinned staging memory), so the caller may reuse it
+ * at once; the call does not wait for the GPU. */
 int si_mpm_set_bodies(si_mpm* h, const float* bodies, int32_t n);
 /* coupling.finish() (coupling.js:199-206, mpm-rigid-apply): the reaction impulses summed since the
  * last read, in world units, n x 8 floats (J xyz, 0, L xyz, 0) — what the reference adds to the
