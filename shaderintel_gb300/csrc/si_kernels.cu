@@ -271,16 +271,24 @@ __device__ __forceinline__ void tile_walk(int ex, int ey, int ez, Fn&& f) {
   }
 }
 
+// A box in shared memory: lo[3], hi[3] of node coordinates, grown with atomicMin/atomicMax. It is
+// emptied by three threads; a CTA barrier must separate that from the atomics that grow it again.
+__device__ __forceinline__ void box_empty(int* b) {
+  if (threadIdx.x < 3) { b[threadIdx.x] = 0x3fffffff; b[3 + threadIdx.x] = -0x3fffffff; }
+}
+
 // CTA-wide P2G: AABB of the bases (mpm.js:353-377), tile if it fits (mpm.js:379-380), scatter,
 // flush of the non-zero tile nodes with global i32 atomics (mpm.js:385-399). The particles come from
 // `reg` (one per thread, valid if has_reg) when sc == nullptr, else from the `count` staged copies.
+// `sbox` arrives empty (and ordered by an earlier barrier); before the final barrier this function
+// empties it again for the next chunk, together with `gbox` (the caller's gather box, or nullptr),
+// once every thread has read them: no barrier is spent on re-initialising either box.
 __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const float* sc, int chunk, int count,
                                             const int32_t* dims, int* __restrict__ grid, bool force_global,
-                                            int tile_nodes, int* tile, int* sbox, int32_t* scene_box, float nz) {
+                                            int tile_nodes, int* tile, int* sbox, int* gbox, int32_t* scene_box,
+                                            float nz) {
   constexpr int tile_cap = kTileNodes;
   const int tid = threadIdx.x;
-  if (tid < 3) { sbox[tid] = 0x3fffffff; sbox[3 + tid] = -0x3fffffff; }
-  cta_sync();
   int lo0 = 0x3fffffff, lo1 = 0x3fffffff, lo2 = 0x3fffffff;
   int hi0 = -0x3fffffff, hi1 = -0x3fffffff, hi2 = -0x3fffffff;
   if (sc == nullptr) {
@@ -309,8 +317,13 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
     atomicMin(&scene_box[0], o0); atomicMin(&scene_box[1], o1); atomicMin(&scene_box[2], o2);
     atomicMax(&scene_box[3], sbox[3]); atomicMax(&scene_box[4], sbox[4]); atomicMax(&scene_box[5], sbox[5]);
   }
-  cta_sync();   // sbox is reused by the next chunk
-  if (ex <= 0 || ey <= 0 || ez <= 0) return;    // no valid particle in the chunk
+  if (ex <= 0 || ey <= 0 || ez <= 0) {   // no valid particle in the chunk (the same for every thread)
+    cta_sync();
+    box_empty(sbox);
+    if (gbox) box_empty(gbox);
+    cta_sync();
+    return;
+  }
   const long long tn = (long long)ex * ey * ez;
   const bool use_tile = tn <= tile_nodes && !force_global;
   const int tnodes = (int)(use_tile ? tn : 0);
@@ -330,8 +343,10 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
       scatter_one(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile, nz);
     }
   }
+  cta_sync();   // every thread has scattered, and has read the boxes long ago
+  box_empty(sbox);
+  if (gbox) box_empty(gbox);
   if (use_tile) {
-    cta_sync();
     tile_walk(ex, ey, ez, [&](int t, int lx, int ly, int lz) {
       const int m = tile[3 * tile_cap + t], mx = tile[t], my = tile[tile_cap + t], mz = tile[2 * tile_cap + t];
       if ((m | mx | my | mz) != 0) {
@@ -355,8 +370,10 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t
   extern __shared__ __align__(16) int smem[];
   int* tile = smem;
   int* sbox = smem + 4 * kTileNodes;
-  float* sc = reinterpret_cast<float*>(sbox + 8);
+  float* sc = reinterpret_cast<float*>(sbox + 16);
   constexpr int chunk = kCtaThreads * PPT;
+  box_empty(sbox);
+  cta_sync();
   for (uint32_t c = blockIdx.x; c < t.pchunks; c += gridDim.x) {
     const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, c)];
     const uint32_t flags = ts.flags;
@@ -380,7 +397,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t
       if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + threadIdx.x, reg);
     }
     cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
-                reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox,
+                reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox, nullptr,
                 ts.box_cur, t.nz);
   }
 }
@@ -700,7 +717,8 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
   F2 = make_float4(F.c[2].x, F.c[2].y, F.c[2].z, t12);
 }
 
-// AABB of the bases of the chunk's particles (x of each slot given by xs), into sbox[0..5].
+// AABB of the bases of the chunk's particles (x of each slot given by xs), into sbox[0..5], which
+// arrives empty (see box_empty) and is complete for every thread on return.
 template <int PPT>
 __device__ __forceinline__ void cta_base_box(const float4 (&xs)[PPT], int count, const int32_t* dims, int* sbox) {
   const int tid = threadIdx.x;
@@ -713,8 +731,6 @@ __device__ __forceinline__ void cta_base_box(const float4 (&xs)[PPT], int count,
     lo0 = min(lo0, b0); lo1 = min(lo1, b1); lo2 = min(lo2, b2);
     hi0 = max(hi0, b0); hi1 = max(hi1, b1); hi2 = max(hi2, b2);
   }
-  if (tid < 3) { sbox[tid] = 0x3fffffff; sbox[3 + tid] = -0x3fffffff; }
-  cta_sync();
   lo0 = __reduce_min_sync(0xffffffffu, lo0); lo1 = __reduce_min_sync(0xffffffffu, lo1);
   lo2 = __reduce_min_sync(0xffffffffu, lo2);
   hi0 = __reduce_max_sync(0xffffffffu, hi0); hi1 = __reduce_max_sync(0xffffffffu, hi1);
@@ -733,10 +749,14 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
   extern __shared__ __align__(16) int smem[];
   int* tile = smem;
   float4* tilef = reinterpret_cast<float4*>(smem);
-  int* sbox = smem + 4 * kTileNodes;
-  float* sc = reinterpret_cast<float*>(sbox + 8);
+  int* gbox = smem + 4 * kTileNodes;   // box of the old stencils (gather tile)
+  int* sbox = gbox + 8;                // box of the new bases (scatter tile)
+  float* sc = reinterpret_cast<float*>(gbox + 16);
   constexpr int chunk = kCtaThreads * PPT;
   const int tid = threadIdx.x;
+  box_empty(gbox);
+  box_empty(sbox);
+  cta_sync();
   for (uint32_t c = blockIdx.x; c < t.pchunks; c += gridDim.x) {
     const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, c)];
     const uint32_t flags = ts.flags;
@@ -762,9 +782,9 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
       js[k] = gather ? (int64_t)__ldg(&perm[ts.seg_base + first + slot]) : (int64_t)(first + slot);
       xs[k] = __ldcs(&Pin[js[k]]);
     }
-    cta_base_box<PPT>(xs, count, dims, sbox);
-    const int o0 = sbox[0], o1 = sbox[1], o2 = sbox[2];
-    const int ex = sbox[3] - o0 + 3, ey = sbox[4] - o1 + 3, ez = sbox[5] - o2 + 3;
+    cta_base_box<PPT>(xs, count, dims, gbox);
+    const int o0 = gbox[0], o1 = gbox[1], o2 = gbox[2];
+    const int ex = gbox[3] - o0 + 3, ey = gbox[4] - o1 + 3, ez = gbox[5] - o2 + 3;
     const long long gtn = (long long)ex * ey * ez;
     const bool gtile = ex > 0 && gtn <= t.tile_nodes;
     // 2. stage the gather tile: vec4f(v, m) of every node under the stencils (zero outside the grid)
@@ -809,13 +829,16 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
         if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + tid, reg);
       }
     }
-    // 4. P2G of the next substep through the same shared memory (cta_scatter synchronises first)
-    if (fuse)
+    // 4. P2G of the next substep through the same shared memory; it empties both boxes for the next
+    // chunk (every thread read gbox before the staging barrier)
+    if (fuse) {
       cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
-                  reinterpret_cast<int*>(ts.grid_next), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox,
+                  reinterpret_cast<int*>(ts.grid_next), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox, gbox,
                   ts.box_next, t.nz);
-    else
+    } else {
+      box_empty(gbox);
       cta_sync();
+    }
   }
 }
 
@@ -887,7 +910,7 @@ __global__ void k_instances(const float4* __restrict__ P, int64_t cap, int64_t o
 // ------------------------------------------------------------------ launchers
 int p2g_smem_bytes(int tile_nodes, int ppt) {
   (void)tile_nodes;
-  return kTileNodes * 16 + 32 + (ppt > 1 ? kScatWords * 4 * kCtaThreads * ppt : 0);
+  return kTileNodes * 16 + 64 + (ppt > 1 ? kScatWords * 4 * kCtaThreads * ppt : 0);
 }
 int max_tile_nodes() { return kTileNodes; }
 
