@@ -271,6 +271,13 @@ __device__ __forceinline__ void tile_walk(int ex, int ey, int ez, Fn&& f) {
   }
 }
 
+// Side of the largest cube of nodes the tile holds (tile_nodes >= 343).
+__device__ __forceinline__ int tile_cube_side(int tile_nodes) {
+  int e = 7;
+  while ((e + 1) * (e + 1) * (e + 1) <= tile_nodes) e++;
+  return e;
+}
+
 // A box in shared memory: lo[3], hi[3] of node coordinates, grown with atomicMin/atomicMax. It is
 // emptied by three threads; a CTA barrier must separate that from the atomics that grow it again.
 __device__ __forceinline__ void box_empty(int* b) {
@@ -310,6 +317,7 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
     atomicMin(&sbox[0], lo0); atomicMin(&sbox[1], lo1); atomicMin(&sbox[2], lo2);
     atomicMax(&sbox[3], hi0); atomicMax(&sbox[4], hi1); atomicMax(&sbox[5], hi2);
   }
+  if (sc == nullptr && tid == kCtaThreads / 2) { sbox[8] = reg.b[0]; sbox[9] = reg.b[1]; sbox[10] = reg.b[2]; }
   cta_sync();
   const int o0 = sbox[0], o1 = sbox[1], o2 = sbox[2];
   const int ex = sbox[3] - o0 + 3, ey = sbox[4] - o1 + 3, ez = sbox[5] - o2 + 3;
@@ -325,32 +333,57 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
     return;
   }
   const long long tn = (long long)ex * ey * ez;
-  const bool use_tile = tn <= tile_nodes && !force_global;
-  const int tnodes = (int)(use_tile ? tn : 0);
+  bool use_tile = tn <= tile_nodes && !force_global;
+  // the tile's box: the chunk's, or (the chunk overflows the tile) the part of it inside a cube of
+  // side e (e^3 <= tile_nodes) around the middle particle's base; particles whose base lies outside
+  // that part scatter with global atomics
+  int t0 = o0, t1 = o1, t2 = o2, tx = ex, ty = ey, tz = ez;
+  bool clipped = false;
+  if (!use_tile && !force_global) {
+    const int e = tile_cube_side(tile_nodes);
+    const int m = (sc == nullptr) ? 0 : count / 2;
+    const int c0 = sc == nullptr ? sbox[8] : __float_as_int(sc[m]);
+    const int c1 = sc == nullptr ? sbox[9] : __float_as_int(sc[chunk + m]);
+    const int c2 = sc == nullptr ? sbox[10] : __float_as_int(sc[2 * chunk + m]);
+    const int half = (e - 3) / 2;
+    const int l0 = max(o0, c0 - half), l1 = max(o1, c1 - half), l2 = max(o2, c2 - half);
+    const int h0 = min(sbox[3], c0 - half + (e - 3)), h1 = min(sbox[4], c1 - half + (e - 3)),
+              h2 = min(sbox[5], c2 - half + (e - 3));
+    if (h0 >= l0 && h1 >= l1 && h2 >= l2) {
+      t0 = l0; t1 = l1; t2 = l2;
+      tx = h0 - l0 + 3; ty = h1 - l1 + 3; tz = h2 - l2 + 3;
+      use_tile = clipped = true;
+    }
+  }
+  const int tnodes = use_tile ? tx * ty * tz : 0;
   if (use_tile) {
     for (int t = tid; t < tnodes; t += blockDim.x) {
       tile[t] = 0; tile[tile_cap + t] = 0; tile[2 * tile_cap + t] = 0; tile[3 * tile_cap + t] = 0;
     }
     cta_sync();
   }
+  auto inside = [&](const Scat& q) {   // the particle's 27 nodes lie in the tile
+    return !clipped || ((unsigned)(q.b[0] - t0) <= (unsigned)(tx - 3) && (unsigned)(q.b[1] - t1) <= (unsigned)(ty - 3) &&
+                        (unsigned)(q.b[2] - t2) <= (unsigned)(tz - 3));
+  };
   if (sc == nullptr) {
-    scatter_one(reg, dims, grid, tile, o0, o1, o2, ex, ey, use_tile, nz);   // every lane (has_reg is true)
+    scatter_one(reg, dims, grid, tile, t0, t1, t2, tx, ty, use_tile && inside(reg), nz);   // every lane
   } else {
 #pragma unroll 1
     for (int slot = tid; slot < count; slot += blockDim.x) {
       Scat s;
       scat_load(sc, chunk, slot, s);
-      scatter_one(s, dims, grid, tile, o0, o1, o2, ex, ey, use_tile, nz);
+      scatter_one(s, dims, grid, tile, t0, t1, t2, tx, ty, use_tile && inside(s), nz);
     }
   }
   cta_sync();   // every thread has scattered, and has read the boxes long ago
   box_empty(sbox);
   if (gbox) box_empty(gbox);
   if (use_tile) {
-    tile_walk(ex, ey, ez, [&](int t, int lx, int ly, int lz) {
+    tile_walk(tx, ty, tz, [&](int t, int lx, int ly, int lz) {
       const int m = tile[3 * tile_cap + t], mx = tile[t], my = tile[tile_cap + t], mz = tile[2 * tile_cap + t];
       if ((m | mx | my | mz) != 0) {
-        const int gx = o0 + lx, gy = o1 + ly, gz = o2 + lz;
+        const int gx = t0 + lx, gy = t1 + ly, gz = t2 + lz;
         if (in_grid(gx, gy, gz, dims)) {
           size_t gi = 4 * ((size_t)gx + (size_t)dims[0] * ((size_t)gy + (size_t)dims[1] * (size_t)gz));
           atomicAdd(&grid[gi], mx);
@@ -370,7 +403,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t
   extern __shared__ __align__(16) int smem[];
   int* tile = smem;
   int* sbox = smem + 4 * kTileNodes;
-  float* sc = reinterpret_cast<float*>(sbox + 16);
+  float* sc = reinterpret_cast<float*>(sbox + 24);
   constexpr int chunk = kCtaThreads * PPT;
   box_empty(sbox);
   cta_sync();
@@ -750,8 +783,8 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
   int* tile = smem;
   float4* tilef = reinterpret_cast<float4*>(smem);
   int* gbox = smem + 4 * kTileNodes;   // box of the old stencils (gather tile)
-  int* sbox = gbox + 8;                // box of the new bases (scatter tile)
-  float* sc = reinterpret_cast<float*>(gbox + 16);
+  int* sbox = gbox + 8;                // box of the new bases (scatter tile) and its middle base
+  float* sc = reinterpret_cast<float*>(gbox + 24);
   constexpr int chunk = kCtaThreads * PPT;
   const int tid = threadIdx.x;
   box_empty(gbox);
@@ -910,7 +943,7 @@ __global__ void k_instances(const float4* __restrict__ P, int64_t cap, int64_t o
 // ------------------------------------------------------------------ launchers
 int p2g_smem_bytes(int tile_nodes, int ppt) {
   (void)tile_nodes;
-  return kTileNodes * 16 + 64 + (ppt > 1 ? kScatWords * 4 * kCtaThreads * ppt : 0);
+  return kTileNodes * 16 + 96 + (ppt > 1 ? kScatWords * 4 * kCtaThreads * ppt : 0);
 }
 int max_tile_nodes() { return kTileNodes; }
 
