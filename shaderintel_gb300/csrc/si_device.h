@@ -99,6 +99,8 @@ struct SortInfo {                // one tick's sort
   uint32_t* keys_b; uint32_t* vals_b;
   uint32_t* hist;                // 256 x tiles
   uint32_t* digit_total;         // 256
+  const uint32_t* keys_in;       // one sorting scene at offset 0: its keys, read by the first pass
+                                 // with identity indices (no concatenation), else nullptr
 };
 
 // ---- launchers (si_kernels.cu / si_sort.cu); all enqueue on `st`.

@@ -382,6 +382,12 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
     s.n = k.sort_n; s.bins = k.sort_bins; s.passes = k.passes;
     s.keys_a = w->ka; s.vals_a = w->va; s.keys_b = w->kb; s.vals_b = w->vb;
     s.hist = w->hist; s.digit_total = w->digit_total;
+    s.keys_in = nullptr;
+    const TickScene* only = nullptr;
+    int sorting = 0;
+    for (const TickScene& e : k.ts)
+      if (e.flags & F_GATHER) { sorting++; only = &e; }
+    if (sorting == 1 && only->seg_base == 0 && only->bin_base == 0) s.keys_in = only->keys;
     launch_sort(t, s, &perm, &skeys, w->ctas_misc, st);
     launch_scene_starts_all(t, skeys, k.max_blocks, st);
     if (k.mode == T_SORT) launch_reorder(t, perm, w->ctas_misc, st);

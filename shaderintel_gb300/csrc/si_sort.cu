@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
 // group's lowest lane), a per-digit prefix over the warps turns the counts into each warp's first
 // position, and a second walk over the same keys stores each at that position plus its rank among
 // the earlier lanes of its round with the same digit. The rank order is (warp, round, lane), which is
-// the keys' order in the tile, so equal digits keep their input order.
+// the keys' order in the tile, so equal digits keep their input order. vin == nullptr stands for the
+// identity (the value of key e is e).
 __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                               uint32_t* kout, uint32_t* vout, uint32_t n, int shift,
                                                               const uint32_t* __restrict__ hist, const uint32_t* __restrict__ digit_total,
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* _
       const uint32_t e = wbase + r * 32 + lane;
       const bool ok = e < n;
       key[r] = ok ? kin[e] : 0u;
-      val[r] = ok ? vin[e] : 0u;
+      val[r] = ok ? (vin ? vin[e] : e) : 0u;
       const uint32_t d = ok ? (key[r] >> shift) & 255u : 256u;
       const unsigned peers = __match_any_sync(0xffffffffu, d);
       if (ok && (peers & lt_mask) == 0u) woff[warp][d] += (uint32_t)__popc(peers);
@@ -205,7 +206,7 @@ void launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
   *perm_out = s.vals_a;
   *keys_out = s.keys_a;
   if (s.n == 0) return;
-  {
+  if (!s.keys_in) {
     int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
     k_sort_init<<<ctas, kCtaThreads, 0, st>>>(t, s.keys_a, s.vals_a);
   }
@@ -214,9 +215,11 @@ void launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
   for (int p = 0; p < s.passes; p++) {
     const int shift = p * kRadixBits;
     int ctas = (int)std::min<uint32_t>(tiles, (uint32_t)grid_ctas);
-    k_radix_hist<<<ctas, kCtaThreads, 0, st>>>(ka, s.n, shift, s.hist, tiles);
+    const uint32_t* kin = (p == 0 && s.keys_in) ? s.keys_in : ka;
+    const uint32_t* vin = (p == 0 && s.keys_in) ? nullptr : va;
+    k_radix_hist<<<ctas, kCtaThreads, 0, st>>>(kin, s.n, shift, s.hist, tiles);
     k_radix_scan<<<256, kCtaThreads, 0, st>>>(s.hist, tiles, s.digit_total);
-    k_radix_scatter<<<ctas, kCtaThreads, 0, st>>>(ka, va, kb, vb, s.n, shift, s.hist, s.digit_total, tiles);
+    k_radix_scatter<<<ctas, kCtaThreads, 0, st>>>(kin, vin, kb, vb, s.n, shift, s.hist, s.digit_total, tiles);
     uint32_t* tk = ka; ka = kb; kb = tk;
     uint32_t* tv = va; va = vb; vb = tv;
   }
