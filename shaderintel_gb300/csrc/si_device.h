@@ -89,6 +89,8 @@ struct TickInfo {                // one tick's totals (kernel arguments)
   int32_t tile_nodes;            // shared tile capacity in nodes
   uint32_t cchunks;              // 4^3 node tiles of the coupled scenes
   float nz;                      // -0.0f: the addend of packed products (see mul2z in si_kernels.cu)
+  uint32_t* grid_done;           // CTAs of k_grid that finished (the last one resets it to 0)
+  int32_t reset_boxes;           // k_grid's last CTA empties every scene's box_next
 };
 
 struct SortInfo {                // one tick's sort

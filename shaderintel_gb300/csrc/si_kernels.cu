@@ -568,6 +568,27 @@ __global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
       if (clear_next) ts.grid_next[i] = make_int4(0, 0, 0, 0);
     }
   }
+  // The CTA that finishes last empties box_next of every scene for the fused P2G of the G2P that
+  // follows: every CTA has read the boxes (grid_region) before it counted itself done.
+  if (t.reset_boxes) {
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last = atomicAdd(t.grid_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+      for (int s = threadIdx.x; s < t.nscenes; s += blockDim.x) {
+        int32_t* b = t.ts[s].box_next;
+        if (b) {
+          b[0] = b[1] = b[2] = 0x3fffffff;
+          b[3] = b[4] = b[5] = -0x3fffffff;
+        }
+      }
+      if (threadIdx.x == 0) *t.grid_done = 0;
+    }
+  }
 }
 
 // Empties box_next of every scene of the tick: the fused P2G of the G2P that follows rebuilds it.

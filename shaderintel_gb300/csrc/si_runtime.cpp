@@ -103,6 +103,8 @@ static int world_init(si_world* w) {
   }
   for (auto& e : w->pev) CK(cudaEventCreate(&e));
   for (auto& e : w->marks) CK(cudaEventCreate(&e));
+  CK(cudaMalloc((void**)&w->grid_done, sizeof(uint32_t)));
+  CK(cudaMemset(w->grid_done, 0, sizeof(uint32_t)));
   return world_configure(w, w->ppt, w->tile_nodes);
 }
 
@@ -349,14 +351,25 @@ static int ensure_sort_scratch(si_world* w, uint32_t n) {
   return SI_OK;
 }
 
+// The one scene a tick sorts, if it sorts exactly one and that one sits at segment and bin 0: its
+// keys feed the first radix pass directly.
+static const TickScene* single_sort_scene(const HostTick& k) {
+  const TickScene* only = nullptr;
+  int sorting = 0;
+  for (const TickScene& e : k.ts)
+    if (e.flags & F_GATHER) { sorting++; only = &e; }
+  return (sorting == 1 && only->seg_base == 0 && only->bin_base == 0) ? only : nullptr;
+}
+
 static int64_t tick_kernels(const HostTick& k) {
   int64_t n = 0;
   if (k.any_keys_now) n++;
-  if (k.any_gather && k.sort_n) n += 2 + 3 * k.passes + (k.mode == T_SORT ? 1 : 0);
+  if (k.any_gather && k.sort_n)
+    n += (single_sort_scene(k) ? 1 : 2) + 3 * k.passes + (k.mode == T_SORT ? 1 : 0);
   if (k.any_clear) n++;
   if (k.any_p2g) n++;
-  if (k.mode == T_SUBSTEP || k.mode == T_GRID) n++;
-  if (k.mode == T_SUBSTEP) n++;   // box reset
+  if ((k.mode == T_SUBSTEP || k.mode == T_GRID) && k.nchunks) n++;
+  if (k.mode == T_SUBSTEP && !k.nchunks) n++;   // box reset by its own kernel when k_grid does not run
   if (k.cchunks) n++;
   if (k.mode == T_SUBSTEP || k.mode == T_G2P) n++;
   return n;
@@ -372,6 +385,8 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   t.chunk = kCtaThreads * w->ppt;
   t.tile_nodes = w->tile_nodes;
   t.nz = -0.0f;
+  t.grid_done = w->grid_done;
+  t.reset_boxes = (k.mode == T_SUBSTEP && k.nchunks > 0) ? 1 : 0;   // else k_box_reset below
   cudaStream_t st = w->st;
   if (profile) cudaEventRecord(w->pev[0], st);
   const uint32_t* perm = nullptr;
@@ -382,12 +397,8 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
     s.n = k.sort_n; s.bins = k.sort_bins; s.passes = k.passes;
     s.keys_a = w->ka; s.vals_a = w->va; s.keys_b = w->kb; s.vals_b = w->vb;
     s.hist = w->hist; s.digit_total = w->digit_total;
-    s.keys_in = nullptr;
-    const TickScene* only = nullptr;
-    int sorting = 0;
-    for (const TickScene& e : k.ts)
-      if (e.flags & F_GATHER) { sorting++; only = &e; }
-    if (sorting == 1 && only->seg_base == 0 && only->bin_base == 0) s.keys_in = only->keys;
+    const TickScene* only = single_sort_scene(k);
+    s.keys_in = only ? only->keys : nullptr;
     launch_sort(t, s, &perm, &skeys, w->ctas_misc, st);
     launch_scene_starts_all(t, skeys, k.max_blocks, st);
     if (k.mode == T_SORT) launch_reorder(t, perm, w->ctas_misc, st);
@@ -398,7 +409,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   if (profile) cudaEventRecord(w->pev[2], st);
   if (k.mode == T_SUBSTEP || k.mode == T_GRID) launch_grid(t, w->ctas_grid, st);
   if (k.cchunks) launch_couple(t, w->sms * 16, st);
-  if (k.mode == T_SUBSTEP) launch_box_reset(t, st);   // box_next starts empty for the fused P2G
+  if (k.mode == T_SUBSTEP && !t.reset_boxes) launch_box_reset(t, st);   // box_next starts empty for the fused P2G
   if (profile) cudaEventRecord(w->pev[3], st);
   if (k.mode == T_SUBSTEP || k.mode == T_G2P) launch_g2p(t, perm, w->ctas_g2p, st);
   if (profile) {
@@ -646,7 +657,7 @@ int si_world_destroy(si_world* w) {
   for (si_mpm* h : sc) scene_release(h);
   world_free_graphs(w);
   for (void* p : {(void*)w->ka, (void*)w->va, (void*)w->kb, (void*)w->vb, (void*)w->hist, (void*)w->digit_total,
-                  (void*)w->tab})
+                  (void*)w->tab, (void*)w->grid_done})
     if (p) cudaFreeAsync(p, w->st);
   cudaStreamSynchronize(w->st);
   for (auto& e : w->pev) if (e) cudaEventDestroy(e);
