@@ -67,7 +67,9 @@ struct TickScene {               // per tick and active scene, host built
   int4* grid_next;               // grid of the next substep
   int32_t* box_cur;              // stencil-base box (min xyz, max xyz) of the P2G that filled `grid`
   int32_t* box_next;             // the same for `grid_next` (the fused P2G of this substep adds to it)
-  uint32_t* keys;                // per-scene key array (pre-sort order)
+  uint32_t* keys;                // block keys this tick's sort reads (pre-sort order; k_keys fills them)
+  uint32_t* keys_next;           // where the G2P writes the keys of the next sort (the other buffer
+                                 // when this tick sorts, so the last sort's keys stay readable)
   uint32_t* starts;              // per-scene starts (num_blocks + 1)
   int64_t cap;                   // stream stride in float4
   int32_t n;                     // particles

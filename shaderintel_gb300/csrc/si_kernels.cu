@@ -875,7 +875,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
         __stcs(&P[i], x); __stcs(&P[cap + i], v); __stcs(&P[2 * cap + i], c0); __stcs(&P[3 * cap + i], c1);
         __stcs(&P[4 * cap + i], c2); __stcs(&P[5 * cap + i], f0); __stcs(&P[6 * cap + i], f1);
         __stcs(&P[7 * cap + i], f2);
-        if (flags & F_KEYS) ts.keys[i] = block_key(x.x, x.y, x.z, prm->num_blocks);
+        if (flags & F_KEYS) ts.keys_next[i] = block_key(x.x, x.y, x.z, prm->num_blocks);
       }
       if (fuse) {
         prep_scatter(reg, x, v, c0, c1, c2, f0.w, f1.w, f2.w, prm);

@@ -62,7 +62,7 @@ static uint32_t num_blocks_for(const int32_t d[3]) {
 }
 
 static int64_t scene_footprint(int64_t cap, int64_t nodes, uint32_t nb) {
-  return 2 * (int64_t)kStreams * 16 * cap + 2 * 16 * nodes + 4 * cap + 4 * ((int64_t)nb + 1) +
+  return 2 * (int64_t)kStreams * 16 * cap + 2 * 16 * nodes + 2 * 4 * cap + 4 * ((int64_t)nb + 1) +
          (int64_t)sizeof(SceneParams) + 64;
 }
 
@@ -244,7 +244,8 @@ static TickScene base_entry(si_mpm* h) {
   t.prm = h->prm;
   t.P = h->pbuf[h->pcur];
   t.Palt = h->pbuf[1 - h->pcur];
-  t.keys = h->keys;
+  t.keys = h->keys[h->kpend];
+  t.keys_next = h->keys[h->kpend];
   t.starts = h->starts;
   t.cap = h->cap;
   t.n = (int32_t)h->count;
@@ -304,6 +305,7 @@ static TickScene substep_entry(si_mpm* h) {
   if (!h->pending) { f |= F_P2G; if (!h->next_clear) f |= F_CLEAR; }
   if (sort_now) { f |= F_GATHER; if (!h->keys_valid) f |= F_KEYS_NOW; }
   if (next_sort) f |= F_KEYS;
+  if (sort_now) t.keys_next = h->keys[1 - h->kpend];   // the sort consumes keys[kpend]
   // both boxes are exact once two standard substeps ran in a row: box_cur from the P2G that filled
   // `grid` (the previous G2P, or the standalone P2G of a substep that started after box_ok was
   // reset), box_next from the one before, whose grid update left values only inside it
@@ -316,7 +318,7 @@ static TickScene substep_entry(si_mpm* h) {
   t.flags = f;
   // state after the substep
   h->gcur = 1 - h->gcur;
-  if (sort_now) h->pcur = 1 - h->pcur;
+  if (sort_now) { h->pcur = 1 - h->pcur; h->kpend = 1 - h->kpend; }
   h->pending = true;
   h->next_clear = false;
   h->keys_valid = next_sort;
@@ -593,7 +595,7 @@ static int run_phase(si_mpm* h, int mode, uint32_t extra_flags) {
   w->use_graphs = g;
   if (r) return r;
   if (mode == T_G2P) invalidate(h);
-  if (mode == T_SORT) { h->pcur = 1 - h->pcur; h->keys_valid = false; }
+  if (mode == T_SORT) { h->pcur = 1 - h->pcur; h->kpend = 1 - h->kpend; h->keys_valid = false; }
   return SI_OK;
 }
 
@@ -633,7 +635,8 @@ static void scene_release(si_mpm* h) {
   if (h->destroyed) return;
   si_world* w = h->w;
   h->destroyed = true;
-  for (void* p : {(void*)h->pbuf[0], (void*)h->pbuf[1], (void*)h->grid[0], (void*)h->grid[1], (void*)h->keys,
+  for (void* p : {(void*)h->pbuf[0], (void*)h->pbuf[1], (void*)h->grid[0], (void*)h->grid[1], (void*)h->keys[0],
+                  (void*)h->keys[1],
                   (void*)h->starts, (void*)h->prm, (void*)h->box, (void*)h->bodies, (void*)h->body_acc})
     if (p) cudaFreeAsync(p, w->st);
   h->bodies = nullptr;
@@ -641,7 +644,7 @@ static void scene_release(si_mpm* h) {
   h->nbodies = 0;
   h->pbuf[0] = h->pbuf[1] = nullptr;
   h->grid[0] = h->grid[1] = nullptr;
-  h->keys = h->starts = nullptr;
+  h->keys[0] = h->keys[1] = h->starts = nullptr;
   h->prm = nullptr;
   h->box = nullptr;
   w->scenes.erase(std::remove(w->scenes.begin(), w->scenes.end(), h), w->scenes.end());
@@ -802,7 +805,8 @@ int scene_create(si_world* w, const si_mpm_desc* in, si_mpm** out, bool own_worl
   cudaError_t e = cudaSuccess;
   for (int b = 0; b < 2 && e == cudaSuccess; b++) e = cudaMallocAsync((void**)&h->pbuf[b], std::max<size_t>(pbytes, 16), st);
   for (int b = 0; b < 2 && e == cudaSuccess; b++) e = cudaMallocAsync((void**)&h->grid[b], (size_t)h->nodes * 16, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->keys, std::max<size_t>(4 * (size_t)h->cap, 16), st);
+  for (int b = 0; b < 2 && e == cudaSuccess; b++)
+    e = cudaMallocAsync((void**)&h->keys[b], std::max<size_t>(4 * (size_t)h->cap, 16), st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->starts, 4 * ((size_t)h->num_blocks + 1), st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->prm, sizeof(SceneParams), st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->box, 64, st);
@@ -1140,7 +1144,7 @@ int si_mpm_device_ptr(si_mpm* h, int32_t what, const void** ptr, int64_t* count,
     *count = h->nodes;
     *stride = 16;
   } else if (what == 9) {
-    *ptr = h->keys;
+    *ptr = h->keys[1 - h->kpend];
     *count = h->count;
     *stride = 4;
   } else if (what == 10) {
@@ -1287,7 +1291,7 @@ int si_mpm_read_grid(si_mpm* h, int32_t* nodes4) {
 int si_mpm_read_bins(si_mpm* h, uint32_t* keys, uint32_t* starts) {
   GUARD(h);
   if (keys && h->count)
-    CK(cudaMemcpyAsync(keys, h->keys, (size_t)h->count * 4, cudaMemcpyDeviceToHost, h->w->st));
+    CK(cudaMemcpyAsync(keys, h->keys[1 - h->kpend], (size_t)h->count * 4, cudaMemcpyDeviceToHost, h->w->st));
   if (starts)
     CK(cudaMemcpyAsync(starts, h->starts, ((size_t)h->num_blocks + 1) * 4, cudaMemcpyDeviceToHost, h->w->st));
   CK(cudaStreamSynchronize(h->w->st));

@@ -106,7 +106,8 @@ struct si_mpm {
   int pcur = 0;
   int4* grid[2] = {nullptr, nullptr};
   int gcur = 0;                     // grid of the last substep
-  uint32_t* keys = nullptr;
+  uint32_t* keys[2] = {nullptr, nullptr};   // block keys: [kpend] for the next sort, the other the last sort's
+  int kpend = 0;
   uint32_t* starts = nullptr;
   int32_t* box = nullptr;           // [2][8]: stencil-base box of the P2G that filled grid[0] / grid[1]
   int box_ok = 0;                   // standard substeps in a row (>= 2: both boxes describe the arrays)
