@@ -129,8 +129,8 @@ int si_mpm_read_particles(si_mpm* h, float* records, int64_t offset, int64_t n);
 int si_mpm_read_instances(si_mpm* h, float* out, int64_t offset, int64_t n, uint32_t mat_mask, double size);
 /* Read-only device views for zero-copy interop (the reference hands layers its GPU buffers, MPM.P /
  * MPM.grid): what = 0..7 particle stream k (float4 per particle: x, v, c0, c1, c2, f0, f1, f2 of the
- * record), 8 the grid of the last grid update (int4 / vec4f per node), 9 the block keys (u32), 10 the
- * starts (u32, numBlocks + 1). *count = elements, *stride = bytes per element. Valid until the next
+ * record), 8 the grid of the last grid update (int4 / vec4f per node), 9 the block keys of the last
+ * sort (u32, pre-sort order, as si_mpm_read_bins), 10 the starts (u32, numBlocks + 1). *count = elements, *stride = bytes per element. Valid until the next
  * call that steps, sorts, adds or destroys; the caller orders its reads after si_mpm_sync. */
 int si_mpm_device_ptr(si_mpm* h, int32_t what, const void** ptr, int64_t* count, int64_t* stride);
 int si_mpm_read_positions(si_mpm* h, float* xyz, int64_t offset, int64_t n);
