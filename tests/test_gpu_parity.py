@@ -295,7 +295,8 @@ def test_sparse_cloud_overflowing_tiles_bit_exact():
 def test_full_size_mixed_scene_bit_exact():
     """The headline scene at full size: 128^3 grid, a 64^3-cell water block and a 24^3-cell jelly
     cube, 8 particles per cell (2,207,744 particles). After two frames, four more substeps (one of
-    them sorting) on the GPU equal the oracle's from the same records, bit for bit, and the block
+    them sorting) on the GPU equal the oracle's from the same records, bit for bit (particles and
+    the grid of the last update), and the block
     bins pass the counting-sort certificate (each block's start span equals its key count)."""
     import os
     g = 128
@@ -308,12 +309,14 @@ def test_full_size_mixed_scene_bit_exact():
     mats, cols, ncol, grav, vol4 = tables(sim)
     rec0 = sim.readParticles()
     sim.step(dt=sim.substepDt, K=4)
-    want, _, sc = O.substeps(rec0, sim.dims, mats, cols, ncol, grav, vol4, 4, step_count=16,
-                             threads=os.cpu_count() or 1)
+    want, wgrid, sc = O.substeps(rec0, sim.dims, mats, cols, ncol, grav, vol4, 4, step_count=16,
+                                 threads=os.cpu_count() or 1)
     assert sim.stepCount == sc == 20
     got = sim.readParticles()
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
         f"{int((got.view(np.uint32) != want.view(np.uint32)).any(1).sum())} particles differ"
+    g = sim.readGrid()
+    assert np.array_equal(g, wgrid), f"{int((g != wgrid).any(1).sum())} grid nodes differ"
     keys, starts = sim.readBins()   # the sort of substep 16 (substep 19 already keyed the next one)
     assert starts[0] == 0 and starts[-1] == sim.count
     counts = np.bincount(keys.astype(np.int64), minlength=len(starts) - 1)
