@@ -708,57 +708,58 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
       t01 = mu0 * (FFt.c[1].x - 0.0f) + l * 0.0f;
       t02 = mu0 * (FFt.c[2].x - 0.0f) + l * 0.0f;
       t12 = mu0 * (FFt.c[2].y - 0.0f) + l * 0.0f;
-    } else if (kind == 2u) {
-      m3 U, Vm; v3 sv;
-      svd3(F, U, sv, Vm);
-      const float lo_s = 1.0f - m1.z, hi_s = 1.0f + m1.w;
-      const v3 s = V(clampf(sv.x, lo_s, hi_s), clampf(sv.y, lo_s, hi_s), clampf(sv.z, lo_s, hi_s));
-      const float Jold = (sv.x * sv.y) * sv.z;
-      const float Jnew = (s.x * s.y) * s.z;
-      vw = clampf((vw * Jold) / Jnew, 0.6f, 20.0f);
-      F = mm(mdiag_right(U, s), mT(Vm));
-      const float h = si_expf(m1.y * (1.0f - vw));
-      const float mu = mu0 * h, la = la0 * h;
-      const m3 R = mm(U, mT(Vm));
-      const float J = Jnew;
-      const float tm = 2.0f * mu;
-      m3 FR;
-      FR.c[0] = vscale(tm, vsub(F.c[0], R.c[0]));
-      FR.c[1] = vscale(tm, vsub(F.c[1], R.c[1]));
-      FR.c[2] = vscale(tm, vsub(F.c[2], R.c[2]));
-      const m3 P1 = mm(FR, mT(F));
-      const float l = (la * J) * (J - 1.0f);
-      t00 = P1.c[0].x + l * 1.0f;
-      t11 = P1.c[1].y + l * 1.0f;
-      t22 = P1.c[2].z + l * 1.0f;
-      t01 = P1.c[1].x + l * 0.0f;
-      t02 = P1.c[2].x + l * 0.0f;
-      t12 = P1.c[2].y + l * 0.0f;
     } else {
+      // snow and sand share one inlined copy of the SVD
       m3 U, Vm; v3 sv;
       svd3(F, U, sv, Vm);
-      v3 e = V(si_logf(fmaxf(fabsf(sv.x), 1e-4f)), si_logf(fmaxf(fabsf(sv.y), 1e-4f)),
-               si_logf(fmaxf(fabsf(sv.z), 1e-4f)));
-      const float tr = (e.x + e.y) + e.z;
-      const float tr3 = tr / 3.0f;
-      const v3 dev = V(e.x - tr3, e.y - tr3, e.z - tr3);
-      const float devn = vlen(dev);
-      if (tr >= 0.0f) {
-        e = V(0.0f, 0.0f, 0.0f);
+      if (kind == 2u) {
+        const float lo_s = 1.0f - m1.z, hi_s = 1.0f + m1.w;
+        const v3 s = V(clampf(sv.x, lo_s, hi_s), clampf(sv.y, lo_s, hi_s), clampf(sv.z, lo_s, hi_s));
+        const float Jold = (sv.x * sv.y) * sv.z;
+        const float Jnew = (s.x * s.y) * s.z;
+        vw = clampf((vw * Jold) / Jnew, 0.6f, 20.0f);
+        F = mm(mdiag_right(U, s), mT(Vm));
+        const float h = si_expf(m1.y * (1.0f - vw));
+        const float mu = mu0 * h, la = la0 * h;
+        const m3 R = mm(U, mT(Vm));
+        const float J = Jnew;
+        const float tm = 2.0f * mu;
+        m3 FR;
+        FR.c[0] = vscale(tm, vsub(F.c[0], R.c[0]));
+        FR.c[1] = vscale(tm, vsub(F.c[1], R.c[1]));
+        FR.c[2] = vscale(tm, vsub(F.c[2], R.c[2]));
+        const m3 P1 = mm(FR, mT(F));
+        const float l = (la * J) * (J - 1.0f);
+        t00 = P1.c[0].x + l * 1.0f;
+        t11 = P1.c[1].y + l * 1.0f;
+        t22 = P1.c[2].z + l * 1.0f;
+        t01 = P1.c[1].x + l * 0.0f;
+        t02 = P1.c[2].x + l * 0.0f;
+        t12 = P1.c[2].y + l * 0.0f;
       } else {
-        const float dg = devn + (((3.0f * la0 + 2.0f * mu0) / (2.0f * mu0)) * tr) * m2.x;
-        if (dg > 0.0f && devn > 1e-12f)
-          e = V(e.x - (dg * dev.x) / devn, e.y - (dg * dev.y) / devn, e.z - (dg * dev.z) / devn);
+        v3 e = V(si_logf(fmaxf(fabsf(sv.x), 1e-4f)), si_logf(fmaxf(fabsf(sv.y), 1e-4f)),
+                 si_logf(fmaxf(fabsf(sv.z), 1e-4f)));
+        const float tr = (e.x + e.y) + e.z;
+        const float tr3 = tr / 3.0f;
+        const v3 dev = V(e.x - tr3, e.y - tr3, e.z - tr3);
+        const float devn = vlen(dev);
+        if (tr >= 0.0f) {
+          e = V(0.0f, 0.0f, 0.0f);
+        } else {
+          const float dg = devn + (((3.0f * la0 + 2.0f * mu0) / (2.0f * mu0)) * tr) * m2.x;
+          if (dg > 0.0f && devn > 1e-12f)
+            e = V(e.x - (dg * dev.x) / devn, e.y - (dg * dev.y) / devn, e.z - (dg * dev.z) / devn);
+        }
+        const v3 s = V(si_expf(e.x), si_expf(e.y), si_expf(e.z));
+        F = mm(mdiag_right(U, s), mT(Vm));
+        const float te = (e.x + e.y) + e.z;
+        const float tm = 2.0f * mu0;
+        const float lt = la0 * te;
+        const v3 dd = V(tm * e.x + lt, tm * e.y + lt, tm * e.z + lt);
+        const m3 T = mm(mdiag_right(U, dd), mT(U));
+        t00 = T.c[0].x; t11 = T.c[1].y; t22 = T.c[2].z;
+        t01 = T.c[1].x; t02 = T.c[2].x; t12 = T.c[2].y;
       }
-      const v3 s = V(si_expf(e.x), si_expf(e.y), si_expf(e.z));
-      F = mm(mdiag_right(U, s), mT(Vm));
-      const float te = (e.x + e.y) + e.z;
-      const float tm = 2.0f * mu0;
-      const float lt = la0 * te;
-      const v3 dd = V(tm * e.x + lt, tm * e.y + lt, tm * e.z + lt);
-      const m3 T = mm(mdiag_right(U, dd), mT(U));
-      t00 = T.c[0].x; t11 = T.c[1].y; t22 = T.c[2].z;
-      t01 = T.c[1].x; t02 = T.c[2].x; t12 = T.c[2].y;
     }
   }
   X = make_float4(nx, ny, nz, X.w);
