@@ -38,9 +38,10 @@ CONFIGS = {
     "dam_break": {"grid": 32, "substeps": 8, "blocks": [("water", [3, 3, 3], [19, 19, 19], [0, 0, 0])],
                   "desc": "dam_break_32: 32^3 grid, 16^3-cell water block at the corner, 8 ppc"},
     "plasticity": {"grid": 96, "substeps": 8, "blocks": [
-        ("snow", [3, 3, 3], [93, 15, 45], [0, 0, 0]),
-        ("sand30", [20, 3, 55], [70, 40, 80], [0, 0, 0])],
-        "desc": "plasticity_96: 96^3 grid, snow slab + Drucker-Prager sand column (friction 30 deg), 8 ppc"},
+        ("snow", [3, 3, 3], [93, 20, 45], [0, 0, 0]),
+        ("sand30", [25, 3, 52], [65, 50, 86], [0, 0, 0])],
+        "desc": "plasticity_96: 96^3 grid, 90x17x42-cell snow slab + 40x47x34-cell Drucker-Prager sand column "
+                "(friction 30 deg), 8 ppc"},
 }
 SAND30 = {"kind": 3, "density": 1.6, "stiffness": 0.6, "poisson": 0.3, "friction": 30}
 
@@ -298,6 +299,35 @@ def fill_scene(sim, s):
     return sim
 
 
+def plasticity_specs(n, seed):
+    """Scenes drawn as the plasticity workload: 96^3 grid, a snow slab on the floor (z below 47) and a
+    Drucker-Prager sand column (friction 30 deg, z from 50) beside it, sizes and x/z placement
+    seeded, 8 ppc: 0.67-1.27 M particles, about 0.94 M on average, half snow and half sand."""
+    import random
+    rng = random.Random(seed)
+    out = []
+    for _ in range(n):
+        slab = [rng.randint(80, 90), rng.randint(14, 20), rng.randint(38, 44)]
+        col = [rng.randint(34, 44), rng.randint(40, 50), rng.randint(30, 36)]
+        lo_s = [3 + rng.randint(0, 90 - slab[0]), 3, 3 + rng.randint(0, 44 - slab[2])]
+        lo_c = [3 + rng.randint(0, 90 - col[0]), 3, 50 + rng.randint(0, 43 - col[2])]
+        out.append({"edge": 96, "blocks": [("snow", lo_s, slab), ("sand30", lo_c, col)],
+                    "seeds": [rng.randrange(1, 1 << 30), rng.randrange(1, 1 << 30)]})
+    return out
+
+
+def plasticity_capacity(s):
+    return sum(8 * (d[0] + 1) * (d[1] + 1) * (d[2] + 1) for _, _, d in s["blocks"])
+
+
+def fill_plasticity(sim, s):
+    e = s["edge"]
+    for (name, lo, size), seed in zip(s["blocks"], s["seeds"]):
+        sim.add({"box": [[x / e for x in lo], [(x + d) / e for x, d in zip(lo, size)]]},
+                material=material_def(name), seed=seed)
+    return sim
+
+
 def b_alg(sims):
     """Algorithmic bytes of one substep of these scenes: 256 B per particle + 32 B per node."""
     return sum(256 * s.count + 32 * s.numNodes for s in sims)
@@ -359,19 +389,28 @@ def run_batched(a, log):
     return out
 
 
-def run_served(a, log):
-    """Continuous batching over up to `serve_resident` resident scenes drawn as the batched workload:
-    Poisson arrivals of step(dt, K) with K uniform in 1..32, admission by a 150 GB budget, scenes
-    retired after 500 substeps and replaced by new ones."""
+def run_served(a, log, scenes="batched"):
+    """Continuous batching over up to `serve_resident` resident scenes drawn as the batched workload
+    (`scenes="batched"`) or as the plasticity workload (`scenes="plasticity"`, about 1 M particles
+    each, so the 150 GB budget is what limits residency): Poisson arrivals of step(dt, K) with K
+    uniform in 1..32, admission by a 150 GB budget, scenes retired after 500 substeps and replaced
+    by new ones. Arrivals stop after `serve_seconds`; every request issued is then waited for."""
     import collections
     import random
     from shaderintel_gb300 import SIError
     from shaderintel_gb300.serving import Server
     rng = random.Random(77)
-    spec_iter = iter(scene_specs(1 << 20, 9191))
+    if scenes == "plasticity":
+        spec_iter = iter(plasticity_specs(1 << 14, 5151))
+        cap_of, fill_of = plasticity_capacity, fill_plasticity
+        drawn = "the plasticity workload (96^3 grid, snow slab + sand column, 0.67-1.27 M particles)"
+    else:
+        spec_iter = iter(scene_specs(1 << 20, 9191))
+        cap_of, fill_of = spec_capacity, fill_scene
+        drawn = "the batched workload"
     srv = Server(budget_bytes=150 * 10 ** 9)
     peak, _ = load_peaks()
-    resident, given, outstanding = [], {}, collections.defaultdict(list)
+    resident, given, size_of, outstanding = [], {}, {}, collections.defaultdict(list)
     retiring = []
     refused = admitted = retired = 0
 
@@ -379,21 +418,27 @@ def run_served(a, log):
         nonlocal refused, admitted
         s = next(spec_iter)
         try:
-            sim = srv.admit(grid=s["edge"], maxParticles=spec_capacity(s), substeps=8)
+            sim = srv.admit(grid=s["edge"], maxParticles=cap_of(s), substeps=8)
         except SIError as e:
             if e.code != "out-of-memory":   # only a full budget is an admission refusal
                 raise
             refused += 1
             return None
-        fill_scene(sim, s)
+        fill_of(sim, s)
         admitted += 1
+        # particles and algorithmic bytes per substep, read once: the properties take the world's
+        # lock, which a round holds while it is enqueued
+        size_of[sim] = (sim.count, 256 * sim.count + 32 * sim.numNodes)
         given[sim] = 0
         resident.append(sim)
         return sim
 
     for _ in range(a.serve_resident):
         admit_one()
-    log(f"served: {len(resident)} resident scenes, {sum(s.count for s in resident)} particles")
+    log(f"served ({scenes}): {len(resident)} resident scenes, {sum(s.count for s in resident)} particles, "
+        f"{refused} refused by the budget")
+    resident_particles = sum(size_of[s][0] for s in resident)
+    issued = 0
     srv.stats(reset=True)
     t0 = time.perf_counter()
     next_t = t0
@@ -413,9 +458,10 @@ def run_served(a, log):
         t = srv.submit(sim, K=K)
         all_tickets.append(t)
         outstanding[sim].append(t)
+        issued += 1
         given[sim] += K
         n_sub += K
-        bytes_done += K * (256 * sim.count + 32 * sim.numNodes)
+        bytes_done += K * size_of[sim][1]
         if given[sim] >= 500:            # retire after 500 substeps: no more requests, then replace
             resident.remove(sim)
             retiring.append(sim)
@@ -429,6 +475,7 @@ def run_served(a, log):
                 srv.retire(r)
                 retiring.remove(r)
                 retired += 1
+    offered = n_sub * (resident_particles / max(1, len(resident))) / max(1e-9, time.perf_counter() - t0)
     for sim, tks in outstanding.items():
         for tk in tks:
             srv.wait(tk, timeout_ms=600000)
@@ -437,8 +484,10 @@ def run_served(a, log):
     srv.destroy()
     thr = st["particle_substeps"] / wall
     return {"workload": f"served: Poisson arrivals {a.serve_rate:g}/s for {a.serve_seconds:g} s over up to "
-                        f"{a.serve_resident} resident scenes drawn as the batched workload, K uniform 1..32, "
+                        f"{a.serve_resident} resident scenes drawn as {drawn}, K uniform 1..32, "
                         "150 GB admission budget, retire after 500 substeps",
+            "resident_scenes": len(resident), "resident_particles": resident_particles,
+            "offered_particle_substeps_per_s": offered, "requests_issued": issued,
             "requests": st["requests_done"], "substeps": st["substeps_done"], "wall_s": wall,
             "value": thr, "unit": "particle-substeps/s", "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
             "mean_ms": st["mean_ms"], "max_ms": st["max_ms"], "busy_s": st["busy_s"],
@@ -597,6 +646,12 @@ def main():
     p.add_argument("--serve-seconds", type=float, default=10.0)
     p.add_argument("--serve-rate", type=float, default=2000.0)
     p.add_argument("--serve-resident", type=int, default=1000)
+    p.add_argument("--no-served-plasticity", action="store_true",
+                   help="skip the served leg over 1 M-particle plasticity scenes")
+    p.add_argument("--serve-p-seconds", type=float, default=2.0,
+                   help="arrival window of each served-plasticity run (every request is then waited for)")
+    p.add_argument("--serve-p-rates", default="2000,200",
+                   help="arrival rates (requests/s) of the served-plasticity runs")
     p.add_argument("--only-batched", action="store_true",
                    help="run the batched leg alone (its line carries the batched metric), e.g. under a profiler")
     p.add_argument("--no-autotune", action="store_true", help="batched leg with the default tuning")
@@ -629,6 +684,12 @@ def main():
         sat = types.SimpleNamespace(serve_rate=max(8000.0, 4 * a.serve_rate), serve_seconds=min(5.0, a.serve_seconds),
                                     serve_resident=a.serve_resident)
         out["served_saturated"] = run_served(sat, log)
+    if world_size == 1 and not a.no_served and not a.no_served_plasticity:
+        import types
+        out["served_plasticity"] = []
+        for rate in (float(x) for x in a.serve_p_rates.split(",") if x):
+            sp = types.SimpleNamespace(serve_rate=rate, serve_seconds=a.serve_p_seconds, serve_resident=1000)
+            out["served_plasticity"].append(run_served(sp, log, scenes="plasticity"))
     if world_size == 1:
         out["conservation"] = run_conservation()
         out["extras"] = run_extras()

@@ -280,8 +280,15 @@ int si_server_destroy(si_server* s);
 int si_server_admit(si_server* s, const si_mpm_desc* desc, si_mpm** out);
 /* Retires a scene (frees its HBM); pending requests on it complete with SI_EDESTROYED. */
 int si_server_retire(si_server* s, si_mpm* h);
-/* Queues step(dt, K) on a resident scene; returns a ticket. */
+/* Queues step(dt, K) on a resident scene; returns a ticket. The scene keeps its collider table. */
 int si_server_submit(si_server* s, si_mpm* h, double dt, int32_t K, uint64_t* ticket);
+/* The same with the collider table that this step uploads (rows of si_collider_row, ncol <= 16
+ * used; ncol = 0 clears the table, ncol < 0 keeps the scene's): the reference's step() uploads its
+ * colliders first (mpm.js:586), and here the table travels with the request, so queued requests of
+ * one scene each run with their own table. It is applied when the request's first substep is
+ * enqueued, and submitting takes no lock that a running round holds. */
+int si_server_submit_colliders(si_server* s, si_mpm* h, double dt, int32_t K, const float* rows, int32_t ncol,
+                               uint64_t* ticket);
 /* *done = 1 once the ticket's K substeps are on the device and finished; *status its result. */
 int si_server_poll(si_server* s, uint64_t ticket, int32_t* done, int32_t* status);
 int si_server_wait(si_server* s, uint64_t ticket, int32_t timeout_ms, int32_t* status);

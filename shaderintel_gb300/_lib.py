@@ -121,6 +121,8 @@ SIGNATURES = {
     "si_server_admit": (ctypes.c_int, [vp, ctypes.POINTER(si_mpm_desc), ctypes.POINTER(vp)]),
     "si_server_retire": (ctypes.c_int, [vp, vp]),
     "si_server_submit": (ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int32, c_uint64_p]),
+    "si_server_submit_colliders": (ctypes.c_int, [vp, vp, ctypes.c_double, ctypes.c_int32, vp, ctypes.c_int32,
+                                                  c_uint64_p]),
     "si_server_poll": (ctypes.c_int, [vp, ctypes.c_uint64, c_int32_p, c_int32_p]),
     "si_server_wait": (ctypes.c_int, [vp, ctypes.c_uint64, ctypes.c_int32, c_int32_p]),
     "si_server_stats_get": (ctypes.c_int, [vp, ctypes.POINTER(si_server_stats), ctypes.c_int32]),

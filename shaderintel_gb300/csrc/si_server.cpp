@@ -34,6 +34,8 @@ struct Request {
   double dt = 0;
   int32_t K = 0;
   int32_t remaining = 0;   // substeps not yet enqueued
+  int32_t ncol = -1;       // the request's collider table (rows below), or -1: keep the scene's
+  std::vector<float> cols;
   Clock::time_point t_submit;
   bool done = false;
   int32_t status = SI_OK;
@@ -114,10 +116,12 @@ static void server_loop(si_server* s) {
     K = std::max(K, 1);
     std::vector<si_mpm*> run;
     std::vector<double> dts;
-    std::vector<Request*> fin;   // the request that this round finishes, per scene (or null)
+    std::vector<Request*> fin;     // the request that this round finishes, per scene (or null)
+    std::vector<Request*> start;   // the request that this round starts, per scene (or null)
     auto* comp = new Completion{s, {}, 0, (int64_t)K};
     for (si_mpm* h : act) {
       Request* r = s->queues[h].front();
+      start.push_back(r->remaining == r->K ? r : nullptr);
       if (r->remaining == r->K) h->frame_sub = 0;   // a request is one step(dt, K) call
       r->remaining -= K;
       fin.push_back(nullptr);
@@ -140,13 +144,23 @@ static void server_loop(si_server* s) {
         size_t k = 0;
         for (size_t i = 0; i < run.size(); i++) {
           if (s->footprint.count(run[i])) {
-            run[k] = run[i]; dts[k] = dts[i]; k++;
+            run[k] = run[i]; dts[k] = dts[i]; start[k] = start[i]; k++;
           } else if (fin[i]) {
             fin[i]->status = SI_EDESTROYED;
           }
         }
         run.resize(k);
         dts.resize(k);
+        start.resize(k);
+      }
+      // a request that starts now brings the collider table that step() would upload (mpm.js:586)
+      for (size_t i = 0; i < run.size(); i++) {
+        const Request* r = start[i];
+        if (!r || r->ncol < 0) continue;
+        std::memset(run[i]->cols, 0, sizeof(run[i]->cols));
+        if (r->ncol) std::memcpy(run[i]->cols, r->cols.data(), sizeof(float) * 12 * (size_t)r->ncol);
+        run[i]->ncol = r->ncol;
+        run[i]->prm_dirty = true;
       }
       for (si_mpm* h : run) comp->particle_substeps += h->count * (int64_t)K;
       // requests carry their own dt: retime before the round when it changes (mpm.js:140-145)
@@ -282,8 +296,19 @@ int si_server_retire(si_server* s, si_mpm* h) {
 }
 
 int si_server_submit(si_server* s, si_mpm* h, double dt, int32_t K, uint64_t* ticket) {
+  return si_server_submit_colliders(s, h, dt, K, nullptr, -1, ticket);
+}
+
+int si_server_submit_colliders(si_server* s, si_mpm* h, double dt, int32_t K, const float* rows, int32_t ncol,
+                               uint64_t* ticket) {
   if (!s || !h || !ticket) return si_fail(SI_EINVAL, "null argument");
   if (K <= 0) return si_fail(SI_EINVAL, "K must be positive");
+  if (ncol > 0 && !rows) return si_fail(SI_EINVAL, "MPM: bad collider table");
+  std::vector<float> cols;
+  if (ncol > 0) {
+    ncol = std::min(ncol, (int32_t)SI_MAX_COLLIDERS);   // colliders.slice(0, 16), mpm.js:280
+    cols.assign(rows, rows + 12 * (size_t)ncol);
+  }
   std::lock_guard<std::mutex> g(s->mu);
   if (s->stop) return si_fail(SI_EDESTROYED, "the server was destroyed");
   auto it = s->queues.find(h);
@@ -294,6 +319,8 @@ int si_server_submit(si_server* s, si_mpm* h, double dt, int32_t K, uint64_t* ti
   r->dt = dt;
   r->K = K;
   r->remaining = K;
+  r->ncol = ncol < 0 ? -1 : ncol;
+  r->cols = std::move(cols);
   r->t_submit = Clock::now();
   s->reqs[r->ticket] = r;
   if (h->count == 0) {   // step() of an empty simulation is a no-op (mpm.js:584)

@@ -7,6 +7,8 @@ admitted only if its device footprint fits the HBM budget.
 """
 import ctypes
 
+import numpy as np
+
 from . import _lib as L
 from ._lib import SIError, check
 from .mpm import MPM, World
@@ -58,11 +60,14 @@ class Server:
     # ---------------------------------------------------------------- requests
     def submit(self, sim, dt=None, K=None):
         """Queues step(dt, K) on `sim` (dt None: its current substep; K None: one frame); returns a
-        ticket. The simulation's colliders are uploaded first, as step() does."""
-        sim._upload_colliders(float(dt) if dt else 0.0)
+        ticket. The request carries the simulation's collider table as step() would upload it, so
+        requests queued on one simulation each run with the colliders they were submitted with."""
+        rows = np.ascontiguousarray(sim._collider_rows(float(dt) if dt else 0.0), np.float32)
         t = ctypes.c_uint64()
         k = int(K) if K else sim.substeps
-        check(L.lib().si_server_submit(self._h, sim._h, float(dt) if dt else 0.0, k, ctypes.byref(t)))
+        check(L.lib().si_server_submit_colliders(self._h, sim._h, float(dt) if dt else 0.0, k,
+                                                 rows.ctypes.data_as(ctypes.c_void_p) if len(rows) else None,
+                                                 len(rows), ctypes.byref(t)))
         return t.value
 
     def poll(self, ticket):

@@ -145,3 +145,44 @@ def test_destroyed_server_rejects_work():
     srv.destroy()
     with pytest.raises(SIError):
         s.step()   # the world and its scenes went with the server it owned
+
+
+def test_queued_requests_keep_their_own_colliders():
+    """A sphere moved between submits: requests queued on one scene each run with the collider
+    table they were submitted with, as the same step(dt, K) calls with setColliders in between."""
+    spec = (32, (4, 3, 5), (20, 12, 18), "water", (1.0, 0.0, 0.5))
+    centers = [(0.40, 0.20, 0.45), (0.46, 0.22, 0.47), (0.52, 0.24, 0.49), (0.58, 0.26, 0.51)]
+    Ks = [5, 3, 7, 4]
+
+    def sphere(c):
+        return [{"type": "sphere", "center": list(c), "radius": 0.12, "velocity": [0.3, 0.1, 0.1]}]
+
+    srv = Server(budget_bytes=4 * 10 ** 9)
+    big = fill(srv.admit(grid=64, maxParticles=400000), (64, (3, 3, 3), (50, 20, 50), "sand", (0, 0, 0)))
+    sim = fill(srv.admit(grid=spec[0], maxParticles=cap_of(spec)), spec)
+    dt = sim.substepDt
+    tb = srv.submit(big, dt=dt, K=16)      # keeps the rounds busy while the others queue
+    tickets = []
+    for c, K in zip(centers, Ks):
+        sim.setColliders(sphere(c))
+        tickets.append(srv.submit(sim, dt=dt, K=K))
+    sim.setColliders([])                   # the queued requests keep their tables
+    for t in tickets + [tb]:
+        assert srv.wait(t, timeout_ms=120000) == 0
+    served = sim.readParticles()
+    srv.destroy()
+
+    ref = fill(MPM(None, grid=spec[0], maxParticles=cap_of(spec), substeps=8), spec)
+    for c, K in zip(centers, Ks):
+        ref.setColliders(sphere(c))
+        ref.step(dt=dt, K=K)
+    want = ref.readParticles()
+    ref.destroy()
+    assert np.array_equal(bits(served), bits(want))
+
+    # and the colliders matter here: the same steps without them end elsewhere
+    free = fill(MPM(None, grid=spec[0], maxParticles=cap_of(spec), substeps=8), spec)
+    for K in Ks:
+        free.step(dt=dt, K=K)
+    assert not np.array_equal(bits(free.readParticles()), bits(want))
+    free.destroy()
