@@ -606,21 +606,26 @@ __global__ void k_box_reset(TickInfo t) {
 // The 27-node gather reads the CTA's shared tile (TILE: node (a,b,c) of the stencil at
 // t0 + a + sx*b + sxy*c, always inside) or, when the CTA's stencils did not fit the tile, the
 // global grid with bounds checks (nodes outside the grid read as zero).
+// The gathered sums of one particle: v += t and B += outer3(t, dpos) with t = wt gv
+// (mpm.js:500-509), product and sum rounded separately, in packed accumulators: (v.x, v.y),
+// (B0.x, B0.y), (B1.x, B1.y), (B2.x, B2.y), (B0.z, B1.z), (v.z, B2.z), where column k of B gains
+// t dpos_k.
+struct Gathered {
+  float2 vxy, bxy0, bxy1, bxy2, z01, z2v;
+};
+
+// The gather over the 27 nodes around a particle, from the shared tile (TILE) or from the grid.
+// Only this part depends on where the nodes come from, so the kernel holds two copies of it and
+// one of the constitutive update below.
 template <bool TILE>
-__device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, float4& C1, float4& C2,
-                                             float4& F0, float4& F1, float4& F2, const SceneParams* prm,
-                                             const float4* __restrict__ grid, const float4* tilef, int o0,
-                                             int o1, int o2, int sx, int sxy, float negz) {
+__device__ __forceinline__ Gathered g2p_gather(const float4& X, const SceneParams* prm,
+                                               const float4* __restrict__ grid, const float4* tilef, int o0,
+                                               int o1, int o2, int sx, int sxy, float negz) {
   const int32_t dx0 = prm->dims[0], dx1 = prm->dims[1], dx2 = prm->dims[2];
   const int b0 = base_of(X.x, dx0), b1 = base_of(X.y, dx1), b2 = base_of(X.z, dx2);
   const float f0 = X.x - (float)b0, f1 = X.y - (float)b1, f2 = X.z - (float)b2;
   float wx[3], wy[3], wz[3];
   bspline(f0, wx); bspline(f1, wy); bspline(f2, wz);
-  v3 v;
-  m3 B;
-  // v += t and B += outer3(t, dpos) with t = wt gv (mpm.js:500-509), product and sum rounded
-  // separately, in packed accumulators: (v.x, v.y), (B0.x, B0.y), (B1.x, B1.y), (B2.x, B2.y),
-  // (B0.z, B1.z), (v.z, B2.z), where column k of B gains t dpos_k.
   float2 vxy = make_float2(0.0f, 0.0f), bxy0 = vxy, bxy1 = vxy, bxy2 = vxy, z01 = vxy, z2v = vxy;
   const int t0 = TILE ? ((b2 - o2) * (sxy / sx) + (b1 - o1)) * sx + (b0 - o0) : 0;
 #pragma unroll 1
@@ -659,6 +664,18 @@ __device__ __forceinline__ void g2p_particle(float4& X, float4& Vv, float4& C0, 
       }
     }
   }
+  return Gathered{vxy, bxy0, bxy1, bxy2, z01, z2v};
+}
+
+// C, velocity clamp, advection and the constitutive update of one particle from its gathered sums
+// (mpm.js:510-558).
+__device__ __forceinline__ void g2p_update(const Gathered& g, float4& X, float4& Vv, float4& C0, float4& C1,
+                                           float4& C2, float4& F0, float4& F1, float4& F2,
+                                           const SceneParams* prm) {
+  const int32_t dx0 = prm->dims[0], dx1 = prm->dims[1], dx2 = prm->dims[2];
+  const float2 vxy = g.vxy, bxy0 = g.bxy0, bxy1 = g.bxy1, bxy2 = g.bxy2, z01 = g.z01, z2v = g.z2v;
+  v3 v;
+  m3 B;
   v = V(vxy.x, vxy.y, z2v.x);
   B.c[0] = V(bxy0.x, bxy0.y, z01.x);
   B.c[1] = V(bxy1.x, bxy1.y, z01.y);
@@ -870,8 +887,10 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
       if (__float_as_uint(__ldg(&prm->mats[(__float_as_uint(x.w) & 7u) * 3].x)) != 0u) {
         f0 = __ldcs(&Pin[5 * cap + j]); f1 = __ldcs(&Pin[6 * cap + j]); f2 = __ldcs(&Pin[7 * cap + j]);
       }
-      if (gtile) g2p_particle<true>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, o0, o1, o2, ex, ex * ey, t.nz);
-      else g2p_particle<false>(x, v, c0, c1, c2, f0, f1, f2, prm, grid, tilef, 0, 0, 0, 1, 1, t.nz);
+      Gathered gs;
+      if (gtile) gs = g2p_gather<true>(x, prm, grid, tilef, o0, o1, o2, ex, ex * ey, t.nz);
+      else gs = g2p_gather<false>(x, prm, grid, tilef, 0, 0, 0, 1, 1, t.nz);
+      g2p_update(gs, x, v, c0, c1, c2, f0, f1, f2, prm);
       if (valid) {
         __stcs(&P[i], x); __stcs(&P[cap + i], v); __stcs(&P[2 * cap + i], c0); __stcs(&P[3 * cap + i], c1);
         __stcs(&P[4 * cap + i], c2); __stcs(&P[5 * cap + i], f0); __stcs(&P[6 * cap + i], f1);
