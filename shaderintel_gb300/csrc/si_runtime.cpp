@@ -1008,10 +1008,19 @@ int si_mpm_emit(si_mpm* h, int32_t shape, const double a[3], const double b[3], 
     cudaFreeAsync(scratch, st);
     return si_fail(SI_EDEVICE, "MPM.add: emission launch failed");
   }
-  uint32_t inside = 0;
-  CK(cudaMemcpyAsync(&inside, scratch + ctas, 4, cudaMemcpyDeviceToHost, st));
-  CK(cudaFreeAsync(scratch, st));
-  CK(cudaStreamSynchronize(st));
+  int64_t inside = e.total;
+  if (shape == 0) {
+    // every lattice point of a box is kept (its inside test is always true, mpm.js:689), so the
+    // count is known here and nothing waits for the stream, which may hold other scenes' substeps
+    // (a server admitting a scene while its rounds run)
+    CK(cudaFreeAsync(scratch, st));
+  } else {
+    uint32_t counted = 0;
+    CK(cudaMemcpyAsync(&counted, scratch + ctas, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaFreeAsync(scratch, st));
+    CK(cudaStreamSynchronize(st));
+    inside = counted;
+  }
   const int64_t n = std::min<int64_t>(inside, room);
   h->count += n;
   invalidate(h);
