@@ -211,7 +211,14 @@ def run_ours(a, rank):
 
     # end to end through the public API with host buffers: every frame uploads the collider table and
     # reads every position back, as readPositions()' Promise: frame k's positions are copied into one
-    # of two pinned buffers while frame k+1 runs, and the loop waits for frame k before queueing k+2
+    # of two pinned buffers while frame k+1 runs, and the loop waits for frame k before queueing k+2.
+    # It runs on a fresh copy of the scene with the same warm-up, so it times the same frames of the
+    # simulation as `value` (a frame's cost changes as the scene evolves)
+    sim.destroy()
+    sim = build_gpu(a.config, world)
+    for _ in range(a.warmup):
+        sim.step()
+    world.sync()
     bufs = [pinned_floats(n_p * 3) for _ in range(2)]
     pinned = bufs[0][1]
     cols, _ = pinned_floats(16 * 12)
