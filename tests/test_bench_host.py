@@ -1,0 +1,68 @@
+"""Host-side parts of bench.py, on CPU: the reference arm's JSON line (the CPU restatement timed on
+the host cores, as `bench.py --impl reference` prints it) and the seeded workload generators of
+the batched and served legs (every block inside the walls, snow and sand apart, capacity enough
+for the emitted lattice)."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+def test_reference_arm_prints_one_contract_line():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--config",
+                        "dam_break", "--steps", "2", "--warmup", "3"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"] == "MPM particle-substeps/s on 1 GB300 (plain single-scene form)"
+    assert d["unit"] == "particle-substeps/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 3
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    e = d["e2e"]
+    assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+    assert d["config"]["particles"] == 32768
+
+
+def _cells(lo, size):
+    return [(lo[a], lo[a] + size[a]) for a in range(3)]
+
+
+def test_batched_scene_draws_stay_inside_the_walls():
+    specs = bench.scene_specs(512, 4242)
+    assert specs == bench.scene_specs(512, 4242)          # seeded
+    for s in specs:
+        e = s["edge"]
+        assert e in bench.BATCH_EDGES and s["material"] in bench.BATCH_MATERIALS
+        for lo, hi in _cells(s["lo"], s["size"]):
+            assert 3 <= lo < hi <= e - 3                   # bound = 3 cells (mpm.js:103)
+        n = 8 * s["size"][0] * s["size"][1] * s["size"][2]
+        assert 0 < n <= bench.spec_capacity(s)
+
+
+def test_plasticity_scene_draws_match_the_workload():
+    specs = bench.plasticity_specs(2000, 5151)
+    assert specs == bench.plasticity_specs(2000, 5151)
+    counts = []
+    for s in specs:
+        assert s["edge"] == 96
+        (m0, lo0, d0), (m1, lo1, d1) = s["blocks"]
+        assert (m0, m1) == ("snow", "sand30")
+        box0, box1 = _cells(lo0, d0), _cells(lo1, d1)
+        for lo, hi in box0 + box1:
+            assert 3 <= lo < hi <= 93
+        assert box0[1][0] == 3 and box1[1][0] == 3       # both on the floor
+        assert box0[2][1] < box1[2][0]                    # the slab and the column do not overlap (z)
+        n = 8 * (d0[0] * d0[1] * d0[2] + d1[0] * d1[1] * d1[2])
+        assert n <= bench.plasticity_capacity(s)
+        counts.append(n)
+    assert 0.6e6 < min(counts) and max(counts) < 1.3e6
+    assert 0.85e6 < sum(counts) / len(counts) < 1.05e6   # about 1 M particles, as the workload asks
