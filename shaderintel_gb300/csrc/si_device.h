@@ -92,6 +92,8 @@ struct TickInfo {                // one tick's totals (kernel arguments)
   uint32_t cchunks;              // 4^3 node tiles of the coupled scenes
   float nz;                      // -0.0f: the addend of packed products (see mul2z in si_kernels.cu)
   uint32_t* grid_done;           // CTAs of k_grid that finished (the last one resets it to 0)
+  uint32_t* g2p_sched;           // k_g2p: [0] chunks handed out past the first wave, [1] CTAs
+                                 // finished (the last one resets both to 0)
   int32_t reset_boxes;           // k_grid's last CTA empties every scene's box_next
 };
 

@@ -826,10 +826,17 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
   float* sc = reinterpret_cast<float*>(gbox + 24);
   constexpr int chunk = kCtaThreads * PPT;
   const int tid = threadIdx.x;
+  // Chunks are handed out in order as CTAs become free: the first wave by CTA index, the rest from a
+  // counter that thread 0 bumps at the start of a chunk for the CTA's next one (chunk costs differ by
+  // up to 2x with the material and the box, so a fixed stride leaves SMs idle at the end). The slot
+  // alternates so that a chunk's write cannot meet a slow warp's read of the previous one.
+  __shared__ uint32_t next_chunk[2];
   box_empty(gbox);
   box_empty(sbox);
   cta_sync();
-  for (uint32_t c = blockIdx.x; c < t.pchunks; c += gridDim.x) {
+  uint32_t parity = 0;
+  for (uint32_t c = blockIdx.x; c < t.pchunks; c = next_chunk[parity], parity ^= 1u) {
+    if (tid == 0) next_chunk[parity] = gridDim.x + atomicAdd(&t.g2p_sched[0], 1u);
     const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, c)];
     const uint32_t flags = ts.flags;
     const SceneParams* prm = ts.prm;
@@ -912,6 +919,16 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
     } else {
       box_empty(gbox);
       cta_sync();
+    }
+  }
+  // every CTA has taken its last (failed) chunk number before it counts itself done, so the last
+  // one out can reset the counters for the next launch
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(&t.g2p_sched[1], 1u) == gridDim.x - 1) {
+      t.g2p_sched[0] = 0;
+      t.g2p_sched[1] = 0;
+      __threadfence();
     }
   }
 }

@@ -103,8 +103,8 @@ static int world_init(si_world* w) {
   }
   for (auto& e : w->pev) CK(cudaEventCreate(&e));
   for (auto& e : w->marks) CK(cudaEventCreate(&e));
-  CK(cudaMalloc((void**)&w->grid_done, sizeof(uint32_t)));
-  CK(cudaMemset(w->grid_done, 0, sizeof(uint32_t)));
+  CK(cudaMalloc((void**)&w->grid_done, 4 * sizeof(uint32_t)));   // k_grid's counter, k_g2p's two
+  CK(cudaMemset(w->grid_done, 0, 4 * sizeof(uint32_t)));
   return world_configure(w, w->ppt, w->tile_nodes);
 }
 
@@ -388,6 +388,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   t.tile_nodes = w->tile_nodes;
   t.nz = -0.0f;
   t.grid_done = w->grid_done;
+  t.g2p_sched = w->grid_done + 1;
   t.reset_boxes = (k.mode == T_SUBSTEP && k.nchunks > 0) ? 1 : 0;   // else k_box_reset below
   cudaStream_t st = w->st;
   if (profile) cudaEventRecord(w->pev[0], st);

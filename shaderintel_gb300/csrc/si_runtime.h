@@ -51,7 +51,8 @@ struct si_world {
   uint32_t* hist = nullptr;
   size_t hist_cap = 0;
   uint32_t* digit_total = nullptr;
-  uint32_t* grid_done = nullptr;    // k_grid's finished-CTA counter (zero between launches)
+  uint32_t* grid_done = nullptr;    // k_grid's finished-CTA counter, then k_g2p's chunk and finished-CTA
+                                    // counters (all zero between launches)
   // tick tables of direct (non-graph) execution
   si::TickScene* tab = nullptr;
   size_t tab_cap = 0;
