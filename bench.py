@@ -447,6 +447,10 @@ def run_served(a, log, scenes="batched"):
     resident_particles = sum(size_of[s][0] for s in resident)
     issued = 0
     srv.stats(reset=True)
+    # the client's own pauses would bunch the Poisson arrivals: no garbage collection while it runs
+    import gc
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     next_t = t0
     n_sub = 0
@@ -483,6 +487,7 @@ def run_served(a, log, scenes="batched"):
                 retiring.remove(r)
                 retired += 1
     offered = n_sub * (resident_particles / max(1, len(resident))) / max(1e-9, time.perf_counter() - t0)
+    gc.enable()
     for sim, tks in outstanding.items():
         for tk in tks:
             srv.wait(tk, timeout_ms=600000)
