@@ -10,8 +10,15 @@ lattices (the reference's own jittered sampler); no dataset is involved.
 One bench step = one frame = the reference's MPM.step() = 8 substeps. `value` is device-timed
 with CUDA events on the library's stream, state resident in HBM (282.6 MB of particle state,
 larger than the 129 MB L2, so no flush is needed between steps). `e2e` is the same metric through
-the public API with host buffers: every frame uploads the 16-row collider table the reference
-uploads each step and reads every particle position back into pinned host memory.
+the public API with host buffers, on a fresh copy of the scene with the same warm-up (so the same
+frames): every frame uploads the 16-row collider table the reference uploads each step and reads
+every particle position back into pinned host memory.
+
+The same line carries the batched form (256 seeded scenes of uneven sizes and materials, one launch
+per phase, autotuned, against the same scenes stepped one by one), the served form (Poisson
+arrivals of step(dt, K) over resident scenes: small scenes at 2,000 and 8,000 requests/s, and
+1 M-particle plasticity scenes under a 150 GB admission budget at 2,000 and 200 requests/s), a
+conservation run of the dam break and a few host-side costs.
 
 `--impl reference` times the reference algorithm on the host cores instead: the CPU restatement
 (oracle/, the reference's WGSL runs only in a browser), all threads, one substep of the same
