@@ -21,7 +21,7 @@ namespace si {
 constexpr int kStreams = 8;           // float4 streams per particle
 constexpr int kCtaThreads = 256;      // threads per CTA of the particle kernels
 constexpr int kMaxPpt = 4;            // particles per thread in one chunk, at most
-constexpr int kNodeChunk = 2048;      // grid nodes per work item of the grid kernel
+constexpr int kNodeChunk = 2048;      // grid nodes per work item of the grid kernel (small grids: fewer)
 constexpr int kSortTile = 4096;       // keys per CTA of a radix pass (256 threads x 16)
 constexpr int kRadixBits = 8;
 
@@ -78,6 +78,7 @@ struct TickScene {               // per tick and active scene, host built
   uint32_t bin_base;             // first global bin of this scene
   uint32_t pchunk_begin;         // first particle chunk of this scene (prefix over the tick)
   uint32_t nchunk_begin;         // first node chunk
+  int32_t node_chunk;            // grid nodes per node chunk of this scene (256..kNodeChunk)
   uint32_t cchunk_begin;         // first 4^3 node tile of the coupling pass
   float lead;                    // coupling: bodies extrapolated by v * lead = (s + 0.5) * dt
 };

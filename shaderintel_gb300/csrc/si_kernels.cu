@@ -442,8 +442,8 @@ __global__ void __launch_bounds__(kCtaThreads) k_clear(TickInfo t) {
     if (!(ts.flags & F_CLEAR)) continue;
     const SceneParams* prm = ts.prm;
     const int64_t nodes = (int64_t)prm->dims[0] * prm->dims[1] * prm->dims[2];
-    const int64_t first = (int64_t)(chunk - ts.nchunk_begin) * kNodeChunk;
-    const int64_t last = min(first + (int64_t)kNodeChunk, nodes);
+    const int64_t first = (int64_t)(chunk - ts.nchunk_begin) * ts.node_chunk;
+    const int64_t last = min(first + (int64_t)ts.node_chunk, nodes);
     for (int64_t i = first + threadIdx.x; i < last; i += blockDim.x) ts.grid[i] = make_int4(0, 0, 0, 0);
   }
 }
@@ -504,9 +504,9 @@ __global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
     const NodeRegion reg = grid_region(ts, prm->dims);
     const uint32_t rxy = (uint32_t)reg.nx * (uint32_t)reg.ny;
     const int64_t nodes = (int64_t)rxy * reg.nz;
-    const int64_t first = (int64_t)(chunk - ts.nchunk_begin) * kNodeChunk;
+    const int64_t first = (int64_t)(chunk - ts.nchunk_begin) * ts.node_chunk;
     if (first >= nodes) continue;
-    const int64_t last = min(first + (int64_t)kNodeChunk, nodes);
+    const int64_t last = min(first + (int64_t)ts.node_chunk, nodes);
     const float bound = prm->bound, ff = prm->floor_friction;
     const float g0 = prm->gravity[0], g1 = prm->gravity[1], g2 = prm->gravity[2];
     const v3 hi = V((float)prm->dims[0] - bound, (float)prm->dims[1] - bound, (float)prm->dims[2] - bound);

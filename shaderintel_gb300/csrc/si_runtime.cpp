@@ -232,6 +232,7 @@ struct HostTick {
   int mode = T_SUBSTEP;
   std::vector<TickScene> ts;
   std::vector<uint32_t> nb, nck, nct;   // per entry: num_blocks, node chunks, coupling tiles (host side)
+  std::vector<int64_t> nodes;           // per entry: grid nodes
   uint32_t pchunks = 0, nchunks = 0, cchunks = 0;
   bool any_p2g = false, any_clear = false, any_gather = false, any_keys_now = false;
   uint32_t sort_n = 0, sort_bins = 0, max_blocks = 0;
@@ -253,6 +254,19 @@ static TickScene base_entry(si_mpm* h) {
 }
 
 static void finish_tick(si_world* w, HostTick& k) {
+  // Nodes per work item of the grid kernels: kNodeChunk, halved (down to one node per thread) while
+  // the whole tick has fewer than 128 items, so that a small scene's grid is spread over many CTAs
+  // instead of a few threads walking many nodes one after another (a tick of many scenes has items
+  // enough at the full size).
+  int64_t all_nodes = 0;
+  for (int64_t n : k.nodes) all_nodes += n;
+  int32_t node_chunk = kNodeChunk;
+  while (node_chunk > kCtaThreads && all_nodes / node_chunk < 128) node_chunk /= 2;
+  k.nck.clear();
+  for (size_t e = 0; e < k.ts.size(); e++) {
+    k.ts[e].node_chunk = node_chunk;
+    k.nck.push_back((uint32_t)((k.nodes[e] + node_chunk - 1) / node_chunk));
+  }
   uint32_t pc = 0, nc = 0, cc = 0, seg = 0, bin = 0;
   const uint32_t chunk = (uint32_t)(kCtaThreads * w->ppt);
   for (size_t e = 0; e < k.ts.size(); e++) {
@@ -288,7 +302,7 @@ static void finish_tick(si_world* w, HostTick& k) {
 static void push_entry(HostTick& k, const si_mpm* h, const TickScene& t) {
   k.ts.push_back(t);
   k.nb.push_back(h->num_blocks);
-  k.nck.push_back((uint32_t)((h->nodes + kNodeChunk - 1) / kNodeChunk));
+  k.nodes.push_back(h->nodes);
   k.nct.push_back((t.flags & F_COUPLE) ? (uint32_t)(((h->dims[0] + 3) / 4) * ((h->dims[1] + 3) / 4) * ((h->dims[2] + 3) / 4)) : 0u);
 }
 
