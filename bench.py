@@ -68,42 +68,54 @@ def load_peaks():
 
 # ----------------------------------------------------------------------------- clocks
 class Clocks:
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    """nvidia-smi sampled every 50 ms from before the timed region to after it. start() and stop()
+    bracket the timed region, and only the samples stamped inside it are reported (all of them if
+    none is, with `in_window` 0)."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index):
         self.proc = None
         self.idx = gpu_index
+        self.t0 = self.t1 = None
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.5)   # let the sampler start before the timed region does
         except OSError:
             self.proc = None
 
+    def start(self):
+        self.t0 = time.time()
+
     def stop(self):
+        self.t1 = time.time()
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.25)
+        time.sleep(0.1)
         self.proc.terminate()
         out, _ = self.proc.communicate(timeout=10)
-        sm, mx, reasons = [], None, set()
+        import datetime
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in out.strip().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                mx = float(f[2])
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(f[2]), float(f[3]), [n for n, v in zip(names, f[6:10]) if v.lower() == "active"]))
             except ValueError:
                 continue
-            for n, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "samples": len(sm),
-                "reasons": sorted(reasons)}
+        lo = (self.t0 if self.t0 is not None else 0.0) - 0.05
+        inside = [r for r in rows if lo <= r[0] <= self.t1 + 0.05]
+        use = inside or rows
+        sm = [r[1] for r in use]
+        reasons = sorted({n for r in use for n in r[3]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": use[-1][2] if use else None,
+                "samples": len(use), "in_window": len(inside), "reasons": reasons}
 
 
 # ----------------------------------------------------------------------------- scenes
@@ -190,11 +202,12 @@ def run_ours(a, rank):
     n_p = sim.count
     nodes = sim.numNodes
     subs = c["substeps"]
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))   # sampling before the warm-up
     for _ in range(a.warmup):
         sim.step()
     world.sync()
     l0 = world.launches()
-    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
     world.mark(0)
     for _ in range(a.steps):
         sim.step()
@@ -362,11 +375,12 @@ def run_batched(a, log):
     else:
         tune = autotune(world, substeps=4, repeats=2)
         log(f"batched: autotune chose {tune['particles_per_cta']}/{tune['tile_nodes']}/{tune['flush']}")
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))   # sampling before the warm-up
     for _ in range(a.warmup):
         world.step(K)
     world.sync()
     l0 = world.launches()
-    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
     world.mark(2)
     for _ in range(a.batch_steps):
         world.step(K)
