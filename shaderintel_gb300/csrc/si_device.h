@@ -108,7 +108,17 @@ struct SortInfo {                // one tick's sort
   uint32_t* digit_total;         // 256
   const uint32_t* keys_in;       // one sorting scene at offset 0: its keys, read by the first pass
                                  // with identity indices (no concatenation), else nullptr
+  uint32_t* starts_out;          // that scene's starts (written by the one-CTA sort), else nullptr
 };
+
+// One sorting scene small enough for the one-CTA sort (k_small_sort): its keys and per-warp bin
+// counters fit in shared memory, and one pass over all bins replaces the radix passes and the
+// starts kernel.
+constexpr uint32_t kSmallSortMaxN = 32768;
+constexpr uint32_t kSmallSortMaxBins = 512;
+inline bool small_sort_ok(uint32_t n, uint32_t bins, bool single) {
+  return single && n > 0 && n <= kSmallSortMaxN && bins > 0 && bins <= kSmallSortMaxBins;
+}
 
 // ---- launchers (si_kernels.cu / si_sort.cu); all enqueue on `st`.
 void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st);
@@ -129,8 +139,8 @@ void launch_positions(const float4* P, int64_t cap, int64_t off, int64_t n, doub
 // Sort of one tick: builds the concatenated (key, index) arrays of the sorting scenes, radix
 // sorts them and leaves perm (sorted source indices, per segment) in *perm_out and the sorted
 // keys in *keys_out.
-void launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out,
-                 const uint32_t** keys_out, int grid_ctas, cudaStream_t st);
+bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out,
+                 const uint32_t** keys_out, int grid_ctas, cudaStream_t st);   // true: starts written
 // Per-scene starts (reference blockCount after the scan) of every sorting scene.
 void launch_scene_starts_all(const TickInfo& t, const uint32_t* sorted_keys, uint32_t max_blocks,
                              cudaStream_t st);

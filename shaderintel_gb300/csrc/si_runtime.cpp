@@ -381,7 +381,9 @@ static int64_t tick_kernels(const HostTick& k) {
   int64_t n = 0;
   if (k.any_keys_now) n++;
   if (k.any_gather && k.sort_n)
-    n += (single_sort_scene(k) ? 1 : 2) + 3 * k.passes + (k.mode == T_SORT ? 1 : 0);
+    n += small_sort_ok(k.sort_n, k.sort_bins, single_sort_scene(k) != nullptr)
+             ? 1 + (k.mode == T_SORT ? 1 : 0)
+             : (single_sort_scene(k) ? 1 : 2) + 3 * k.passes + (k.mode == T_SORT ? 1 : 0);
   if (k.any_clear) n++;
   if (k.any_p2g) n++;
   if ((k.mode == T_SUBSTEP || k.mode == T_GRID) && k.nchunks) n++;
@@ -416,8 +418,8 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
     s.hist = w->hist; s.digit_total = w->digit_total;
     const TickScene* only = single_sort_scene(k);
     s.keys_in = only ? only->keys : nullptr;
-    launch_sort(t, s, &perm, &skeys, w->ctas_misc, st);
-    launch_scene_starts_all(t, skeys, k.max_blocks, st);
+    s.starts_out = only ? only->starts : nullptr;
+    if (!launch_sort(t, s, &perm, &skeys, w->ctas_misc, st)) launch_scene_starts_all(t, skeys, k.max_blocks, st);
     if (k.mode == T_SORT) launch_reorder(t, perm, w->ctas_misc, st);
   }
   if (profile) cudaEventRecord(w->pev[1], st);

@@ -201,11 +201,101 @@ __global__ void k_scene_starts(TickInfo t, const uint32_t* __restrict__ skeys) {
   }
 }
 
-void launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out, const uint32_t** keys_out,
+// The block binning of one small scene by one CTA in a single pass over all bins (at most 512 bins
+// and 32768 keys, which fit in shared memory with 32 warps' counters). It ranks the keys as
+// k_radix_scatter does, per warp over a contiguous segment, so the order is the stable one of the
+// radix sort; the scan over the bins gives the scene's starts (scan.js:288-306) directly.
+constexpr int kSmallThreads = 1024;
+constexpr int kSmallWarps = kSmallThreads / 32;
+
+__global__ void __launch_bounds__(kSmallThreads, 1) k_small_sort(const uint32_t* __restrict__ kin, uint32_t n,
+                                                                 uint32_t bins, uint32_t* kout, uint32_t* vout,
+                                                                 uint32_t* starts) {
+  extern __shared__ uint32_t ss[];
+  __shared__ uint32_t wsum[kSmallWarps];
+  uint32_t* keys = ss;                                 // n keys
+  const uint32_t row = bins + 1;                       // bin `bins`: lanes past the end (never counted)
+  uint32_t* cnt = ss + n;                              // kSmallWarps x row counters
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (uint32_t i = tid; i < n; i += kSmallThreads) {
+    const uint32_t k = kin[i];
+    keys[i] = k < bins ? k : bins - 1;                 // block keys are < bins; kept in range regardless
+  }
+  for (uint32_t i = tid; i < (uint32_t)kSmallWarps * row; i += kSmallThreads) cnt[i] = 0;
+  __syncthreads();
+  const uint32_t seg = ((n + kSmallWarps - 1) / kSmallWarps + 31u) & ~31u;   // whole rounds of 32
+  const uint32_t wb = (uint32_t)warp * seg, we = min(n, wb + seg);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  uint32_t* wc = cnt + (uint32_t)warp * row;
+  // 1. the warp's bin counts
+  for (uint32_t base = wb; base < wb + seg; base += 32) {
+    const uint32_t e = base + lane;
+    const bool ok = e < we;
+    const uint32_t d = ok ? keys[e] : bins;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (ok && (peers & lt_mask) == 0u) wc[d] += (uint32_t)__popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  // 2. starts: exclusive scan of the bin totals (thread b: bin b); then each warp's first position
+  uint32_t tot = 0;
+  if ((uint32_t)tid < bins)
+    for (int w = 0; w < kSmallWarps; w++) tot += cnt[(uint32_t)w * row + tid];
+  uint32_t x = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  uint32_t pre = 0;
+  for (int w = 0; w < warp; w++) pre += wsum[w];
+  if ((uint32_t)tid < bins) {
+    uint32_t acc = pre + x - tot;
+    starts[tid] = acc;
+    for (int w = 0; w < kSmallWarps; w++) {
+      const uint32_t c = cnt[(uint32_t)w * row + tid];
+      cnt[(uint32_t)w * row + tid] = acc;
+      acc += c;
+    }
+  }
+  if (tid == 0) starts[bins] = n;
+  __syncthreads();
+  // 3. ranks and stores, in the order of the counts
+  for (uint32_t base = wb; base < wb + seg; base += 32) {
+    const uint32_t e = base + lane;
+    const bool ok = e < we;
+    const uint32_t d = ok ? keys[e] : bins;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t rank = (uint32_t)__popc(peers & lt_mask);
+    const uint32_t at = ok ? wc[d] : 0u;
+    __syncwarp();
+    if (ok) {
+      kout[at + rank] = d;
+      vout[at + rank] = e;
+      if (rank == 0) wc[d] = at + (uint32_t)__popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out, const uint32_t** keys_out,
                  int grid_ctas, cudaStream_t st) {
   *perm_out = s.vals_a;
   *keys_out = s.keys_a;
-  if (s.n == 0) return;
+  if (s.n == 0) return false;
+  if (s.keys_in && s.starts_out && small_sort_ok(s.n, s.bins, true)) {
+    const int smem = (int)((s.n + (uint32_t)kSmallWarps * (s.bins + 1)) * sizeof(uint32_t));
+    static bool attr_set = false;   // the largest case, once per process
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_small_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)((kSmallSortMaxN + (uint32_t)kSmallWarps * (kSmallSortMaxBins + 1)) * sizeof(uint32_t)));
+      attr_set = true;
+    }
+    k_small_sort<<<1, kSmallThreads, smem, st>>>(s.keys_in, s.n, s.bins, s.keys_a, s.vals_a, s.starts_out);
+    return true;
+  }
   if (!s.keys_in) {
     int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
     k_sort_init<<<ctas, kCtaThreads, 0, st>>>(t, s.keys_a, s.vals_a);
@@ -225,6 +315,7 @@ void launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
   }
   *perm_out = va;
   *keys_out = ka;
+  return false;
 }
 
 void launch_scene_starts_all(const TickInfo& t, const uint32_t* sorted_keys, uint32_t max_blocks, cudaStream_t st) {
