@@ -287,12 +287,11 @@ bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
   if (s.n == 0) return false;
   if (s.keys_in && s.starts_out && small_sort_ok(s.n, s.bins, true)) {
     const int smem = (int)((s.n + (uint32_t)kSmallWarps * (s.bins + 1)) * sizeof(uint32_t));
-    static bool attr_set = false;   // the largest case, once per process
-    if (!attr_set) {
+    static std::once_flag attr_once;   // the largest case, once per process (worlds may sort from several threads)
+    std::call_once(attr_once, [] {
       cudaFuncSetAttribute(k_small_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)((kSmallSortMaxN + (uint32_t)kSmallWarps * (kSmallSortMaxBins + 1)) * sizeof(uint32_t)));
-      attr_set = true;
-    }
+    });
     k_small_sort<<<1, kSmallThreads, smem, st>>>(s.keys_in, s.n, s.bins, s.keys_a, s.vals_a, s.starts_out);
     return true;
   }
