@@ -182,7 +182,9 @@ int si_mpm_sync(si_mpm* h);
  * kept until the process exits): n may be at most 262144, larger n fails with SI_EINVAL. Every
  * call uses the same array, so calls that overlap on the GPU (other streams, other threads) race:
  * order them. The first call on each device looks up the array's address; make that first call
- * before any stream capture. No part of the scratch needs to start at zero. */
+ * before any stream capture. That address is kept for the life of the process: do not call this
+ * after a cudaDeviceReset (or any other reset of the device's primary context), which reloads the
+ * library's device code elsewhere. No part of the scratch needs to start at zero. */
 int si_block_sort_noalloc(const float* x, int64_t stride_floats, int32_t n, const int32_t dims[3],
                           uint32_t* keys, uint32_t* perm, uint32_t* starts, void* stream);
 

@@ -144,6 +144,8 @@ bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
 // Per-scene starts (reference blockCount after the scan) of every sorting scene.
 void launch_scene_starts_all(const TickInfo& t, const uint32_t* sorted_keys, uint32_t max_blocks,
                              cudaStream_t st);
+// Per-device kernel attributes (dynamic shared memory opt-ins), set with the device current.
+cudaError_t configure_sort_kernels();
 int p2g_smem_bytes(int tile_nodes, int ppt);
 int max_tile_nodes();
 int occupancy_ctas(int which, int tile_nodes, int ppt);   // resident CTAs per SM of kernel `which`

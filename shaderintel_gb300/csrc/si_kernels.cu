@@ -1006,12 +1006,14 @@ int p2g_smem_bytes(int tile_nodes, int ppt) {
 int max_tile_nodes() { return kTileNodes; }
 
 template <int PPT>
-static void set_smem_attr(int tile_nodes) {
+static cudaError_t set_smem_attr(int tile_nodes) {
   int bytes = p2g_smem_bytes(tile_nodes, PPT);
   if (bytes > 48 * 1024) {
-    cudaFuncSetAttribute(k_p2g<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_g2p<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_p2g<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_g2p<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   }
+  return cudaSuccess;
 }
 
 void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st) {
@@ -1087,10 +1089,14 @@ void launch_positions(const float4* P, int64_t cap, int64_t off, int64_t n, doub
   k_positions<<<ctas, 256, 0, st>>>(P, off, n, dx, origin[0], origin[1], origin[2], xyz);
 }
 
-void configure_kernels(int tile_nodes) {
-  set_smem_attr<1>(tile_nodes);
-  set_smem_attr<2>(tile_nodes);
-  set_smem_attr<4>(tile_nodes);
+// Shared-memory opt-ins of the substep kernels and of the one-CTA sort, on the current device (the
+// world's): an attribute set on one device does not carry over to another.
+cudaError_t configure_kernels(int tile_nodes) {
+  cudaError_t e = set_smem_attr<1>(tile_nodes);
+  if (e == cudaSuccess) e = set_smem_attr<2>(tile_nodes);
+  if (e == cudaSuccess) e = set_smem_attr<4>(tile_nodes);
+  if (e == cudaSuccess) e = configure_sort_kernels();
+  return e;
 }
 
 int occupancy_ctas(int which, int tile_nodes, int ppt) {

@@ -112,9 +112,20 @@ int world_configure(si_world* w, int ppt, int tile_nodes) {
   if (ppt != 1 && ppt != 2 && ppt != 4) return si_fail(SI_EINVAL, "particles per CTA must be 256, 512 or 1024");
   if (tile_nodes < 343 || tile_nodes > max_tile_nodes() || p2g_smem_bytes(tile_nodes, ppt) > w->max_smem_optin)
     return si_fail(SI_EINVAL, "tile capacity must hold at least 7^3 nodes and fit shared memory");
+  {
+    // kernel attributes are per device: set them on the world's, whichever device this thread has current
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) cur = -1;
+    if (cur != w->device) CK(cudaSetDevice(w->device));
+    const cudaError_t e = configure_kernels(tile_nodes);
+    if (cur >= 0 && cur != w->device) cudaSetDevice(cur);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return si_fail(SI_EDEVICE, "setting the kernels' shared-memory attributes failed");
+    }
+  }
   w->ppt = ppt;
   w->tile_nodes = tile_nodes;
-  configure_kernels(tile_nodes);
   const int which_g2p = ppt == 1 ? 3 : (ppt == 4 ? 4 : 1);
   w->ctas_p2g = w->sms * occupancy_ctas(0, tile_nodes, ppt);
   w->ctas_g2p = w->sms * occupancy_ctas(which_g2p, tile_nodes, ppt);

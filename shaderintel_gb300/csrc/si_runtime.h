@@ -135,5 +135,5 @@ int scene_create(si_world* w, const si_mpm_desc* in, si_mpm** out, bool own_worl
 int64_t scene_footprint_of(const si_mpm_desc* in);
 
 namespace si {
-void configure_kernels(int tile_nodes);
+cudaError_t configure_kernels(int tile_nodes);   // per device, with it current
 }

@@ -12,6 +12,7 @@
 
 #include "si_cuda.h"
 #include "si_device.h"
+#include "si_math.cuh"
 
 namespace si {
 
@@ -280,18 +281,22 @@ __global__ void __launch_bounds__(kSmallThreads, 1) k_small_sort(const uint32_t*
   }
 }
 
+// Opts k_small_sort in to the dynamic shared memory of its largest case (about 192 KB). The
+// attribute belongs to the device that is current, so every world calls this on its own device.
+cudaError_t configure_sort_kernels() {
+  return cudaFuncSetAttribute(k_small_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)((kSmallSortMaxN + (uint32_t)kSmallWarps * (kSmallSortMaxBins + 1)) *
+                                    sizeof(uint32_t)));
+}
+
 bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out, const uint32_t** keys_out,
                  int grid_ctas, cudaStream_t st) {
   *perm_out = s.vals_a;
   *keys_out = s.keys_a;
   if (s.n == 0) return false;
   if (s.keys_in && s.starts_out && small_sort_ok(s.n, s.bins, true)) {
+    // the shared-memory opt-in of the largest case was set on this device by configure_sort_kernels()
     const int smem = (int)((s.n + (uint32_t)kSmallWarps * (s.bins + 1)) * sizeof(uint32_t));
-    static std::once_flag attr_once;   // the largest case, once per process (worlds may sort from several threads)
-    std::call_once(attr_once, [] {
-      cudaFuncSetAttribute(k_small_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)((kSmallSortMaxN + (uint32_t)kSmallWarps * (kSmallSortMaxBins + 1)) * sizeof(uint32_t)));
-    });
     k_small_sort<<<1, kSmallThreads, smem, st>>>(s.keys_in, s.n, s.bins, s.keys_a, s.vals_a, s.starts_out);
     return true;
   }
@@ -343,19 +348,7 @@ __global__ void k_na_keys(const float* __restrict__ x, int64_t stride, int32_t n
                           uint32_t* keys_out, uint32_t* skeys, uint32_t* svals) {
   for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float* p = x + (int64_t)i * stride;
-    const float fx = fminf(fmaxf(p[0], 0.0f), 16777216.0f), fy = fminf(fmaxf(p[1], 0.0f), 16777216.0f);
-    const float fz = fminf(fmaxf(p[2], 0.0f), 16777216.0f);
-    const uint32_t bx = ((uint32_t)fx) / 4u, by = ((uint32_t)fy) / 4u, bz = ((uint32_t)fz) / 4u;
-    auto part = [](uint32_t v) {
-      v &= 0x3ffu;
-      v = (v | (v << 16)) & 0x030000ffu;
-      v = (v | (v << 8)) & 0x0300f00fu;
-      v = (v | (v << 4)) & 0x030c30c3u;
-      v = (v | (v << 2)) & 0x09249249u;
-      return v;
-    };
-    uint32_t k = part(bx) | (part(by) << 1) | (part(bz) << 2);
-    k = k < num_blocks ? k : num_blocks - 1u;
+    const uint32_t k = block_key(p[0], p[1], p[2], num_blocks);   // the key of si_mpm_sort, one definition
     keys_out[i] = k;
     skeys[i] = k;
     svals[i] = (uint32_t)i;

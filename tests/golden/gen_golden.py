@@ -1,8 +1,9 @@
 """Makes the golden fixtures of tests/golden/ by executing the reference's own WGSL (TEST INFRASTRUCTURE).
 
-Run in a checkout that has the reference beside it:
-    python tests/golden/gen_golden.py /root/reference
-It reads src/physics/mpm.js and src/shaders/linalg.js, builds each MPM kernel the way the
+Run with the path of a reference checkout (v0.3.0) as the argument, or in SI_REFERENCE_DIR:
+    python tests/golden/gen_golden.py <reference checkout> [--couple | --retime | --spatial]
+It reads src/physics/mpm.js and src/shaders/linalg.js (and, for the extra fixtures,
+src/physics/coupling.js, src/physics/rigid-wgsl.js, src/shaders/math.js, src/prims/grid.js), builds each MPM kernel the way the
 reference's Kernel class wraps it (src/core/kernel.js:83-104: `let wgi = wid.x + wid.y * nwg.x;
 let i = wgi * WG + lidx;` and the `i >= u.n` guard), with the template values of a device without
 subgroups and with 16 KB of workgroup memory (tileCap = (16384 - 512) / 16 = 992, mpm.js:302), and
@@ -310,10 +311,82 @@ def main_couple(ref):
     print("couple", moved, "nodes changed; acc", out["acc"].reshape(-1, 8)[:, [0, 1, 2, 4, 5, 6]].tolist())
 
 
+# ============================================================================ retime (mpm-retime)
+def main_retime(ref):
+    """rescaleK of mpm.js:405-413 (run by _retime, mpm.js:140-145) on a deformed five-material state,
+    from the same state at k = 0.5, k = 2 and the k of a substeps change 8 -> 6 (f64 ratio of the
+    two substepDt values, rounded to f32 as the uniform is)."""
+    mods, kern = kernel_sources(ref)
+    shared, code = kern["mpm-retime"]
+    g, rec, mats, _ = scene_records(16, [
+        ({"box": [[0.3, 0.3, 0.3], [0.45, 0.45, 0.45]]}, dict(kind=0, density=1, stiffness=1.0, viscosity=0.0), [0, 0, 0]),
+        ({"box": [[0.5, 0.3, 0.3], [0.62, 0.42, 0.42]]}, dict(kind=0, density=1.4, stiffness=0.9, viscosity=1.0), [0, 0, 0]),
+        ({"box": [[0.3, 0.5, 0.3], [0.42, 0.62, 0.42]]}, dict(kind=1, density=1, stiffness=0.35, poisson=0.3), [0, 0, 0]),
+        ({"box": [[0.5, 0.5, 0.3], [0.62, 0.62, 0.42]]}, dict(kind=2, density=0.4, stiffness=0.6, poisson=0.2, hardening=10, compression=0.025, stretch=0.0075), [0, 0, 0]),
+        ({"box": [[0.4, 0.4, 0.5], [0.52, 0.52, 0.62]]}, dict(kind=3, density=1.6, stiffness=0.6, poisson=0.3, friction=30), [0, 0, 0])])
+    rec = randomise(rec, 13, scale=0.7, deform=True)
+    ns = compile_kernel(mods, shared, code, g["dims"], guard=True)
+    k86 = ((1 / 60) * 1 / 6) / ((1 / 60) * 1 / 8)
+    ks = np.array([0.5, 2.0, k86], np.float32)
+    outs = []
+    for k in ks:
+        P = W.Buffer(np.ascontiguousarray(rec, np.float32).reshape(-1, 4).copy(), "f32", 4)
+        W.dispatch(ns, math.ceil(len(rec) / WG), WG, {"P": P}, {"n": np.uint32(len(rec)), "k": np.float32(k)})
+        outs.append(P.arr.reshape(-1, 32).copy())
+    np.savez_compressed(os.path.join(HERE, "retime.npz"), rec=rec, mats=mats, dims=np.array(g["dims"]), ks=ks,
+                        out=np.stack(outs))
+    print("retime", rec.shape, ks.tolist())
+
+
+# ============================================================================ SpatialGrid (grid.js)
+def main_spatial(ref):
+    """SpatialGrid.build of src/prims/grid.js:23-96: grid-count (gridCoord / gridIndex of the 'grid'
+    module, atomic ranks), the exclusive scan of the counts with the total in element numCells
+    (scan.js:288-306), grid-scatter. Points include some outside the box (gridCoord clamps them)."""
+    src = open(os.path.join(ref, "src/prims/grid.js")).read()
+    mod = W.field_template(src, "defineModule('grid'", "code")
+    count_code = W.field_template(src, "name: 'grid-count'", "code")
+    scatter_code = W.field_template(src, "name: 'grid-scatter'", "code")
+    rng = np.random.default_rng(21)
+    lo, hi, cell = [-1.0, 0.0, 0.5], [1.0, 1.5, 1.7], 0.125
+    dims = [max(1, math.ceil((hi[a] - lo[a]) / cell)) for a in range(3)]
+    cells = dims[0] * dims[1] * dims[2]
+    n = 2500
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = rng.uniform(np.array(lo) - 0.1, np.array(hi) + 0.1, (n, 3)).astype(np.float32)
+    pos[:40, :3] = pos[0, :3]                              # one crowded cell
+    uni = {"n": np.uint32(n), "gridOrigin": W.Vec(np.array(lo, np.float32)), "gridInv": np.float32(1 / cell),
+           "gridDims": W.Vec(np.array(dims, np.uint32)), "gridCells": np.uint32(cells)}
+    pre = "let i = wgi * WG + lidx;\nif (i >= u.n) { return; }\n"
+    ns = W.compile_module(f"const WG = {WG}u;\n" + mod, pre + count_code)
+    cellb = W.Buffer(np.zeros(n, np.uint32), "u32", 1)
+    rankb = W.Buffer(np.zeros(n, np.uint32), "u32", 1)
+    cnt = W.Buffer(np.zeros(cells + 1, np.uint32), "u32", 1)
+    W.dispatch(ns, math.ceil(n / WG), WG, {"pos": W.Buffer(pos.copy(), "f32", 4), "cell": cellb, "rank": rankb,
+                                           "count": cnt}, uni)
+    counts = cnt.arr.copy()
+    start = np.concatenate([[0], np.cumsum(counts[:-1])]).astype(np.uint32)
+    ns2 = W.compile_module(f"const WG = {WG}u;\n", pre + scatter_code)
+    order = W.Buffer(np.zeros(n, np.uint32), "u32", 1)
+    W.dispatch(ns2, math.ceil(n / WG), WG, {"cell": cellb, "rank": rankb, "start": W.Buffer(start.copy(), "u32", 1),
+                                            "order": order}, {"n": np.uint32(n)})
+    np.savez_compressed(os.path.join(HERE, "spatial.npz"), pos=pos, lo=np.array(lo), hi=np.array(hi), cell_size=cell,
+                        dims=np.array(dims), cell=cellb.arr.copy(), start=start, order=order.arr.copy())
+    print("spatial", n, "points", cells, "cells")
+
+
 if __name__ == "__main__":
-    ref_dir = next((a for a in sys.argv[1:] if not a.startswith("--")), "/root/reference")
+    ref_dir = next((a for a in sys.argv[1:] if not a.startswith("--")), os.environ.get("SI_REFERENCE_DIR"))
+    if not ref_dir:
+        sys.exit("usage: gen_golden.py <reference checkout> [--couple|--retime|--spatial] (or set SI_REFERENCE_DIR)")
     if "--couple" in sys.argv:
         main_couple(ref_dir)
+    elif "--retime" in sys.argv:
+        main_retime(ref_dir)
+    elif "--spatial" in sys.argv:
+        main_spatial(ref_dir)
     else:
         main(ref_dir)
         main_couple(ref_dir)
+        main_retime(ref_dir)
+        main_spatial(ref_dir)

@@ -10,6 +10,10 @@ What the fixtures hold (tests/golden/gen_golden.py makes them, with the referenc
   trajectory.npz  12 substeps of step()'s schedule (sort every 4th) for water and honey
   couple.npz      the fluid <-> rigid coupling pass and apply (src/physics/coupling.js) on a pool with
                   five bodies (dynamic sphere and rotated box, static capsule, disabled, masked out)
+  retime.npz      mpm-retime (mpm.js:405-413) on a deformed five-material state at k = 0.5, 2 and the
+                  k of a substeps change 8 -> 6
+  spatial.npz     SpatialGrid.build (src/prims/grid.js:23-96): cells, starts and order of 2,500 points,
+                  some outside the box and 40 in one cell
 
 Bar: bit-exact for keys, starts, sorted records, grid sums, the grid update and every particle
 field whose computation has no log/exp. log and exp are implementation-defined in WGSL (absolute
@@ -209,3 +213,79 @@ def test_oracle_coupling_matches_reference_wgsl():
     ext, rest = O.couple_apply(acc, len(d["bodies"]), float(d["mom_to_world"]), float(d["params"][3]))
     assert np.array_equal(bits(ext), bits(d["ext"]))
     assert not rest.any()
+
+
+# ---------------------------------------------------------------------------- retime (mpm.js:136-145, 405-413)
+
+
+def test_oracle_retime_matches_reference_wgsl():
+    d = fixture("retime.npz")
+    for k, want in zip(d["ks"], d["out"]):
+        got = O.retime(d["rec"], float(k))
+        assert np.array_equal(bits(got), bits(want)), f"k = {k}"
+    assert not np.array_equal(bits(d["out"][0]), bits(d["rec"]))
+
+
+@pytest.mark.gpu
+def test_cuda_retime_matches_reference_wgsl():
+    """The substep-length change through the C ABI: si_mpm_set_substep_dt at half and twice the
+    substep, and the substeps setter 8 -> 6 (si_mpm_set_frame), each from the fixture's state, equal
+    the reference's mpm-retime output and the oracle's sio_retime bit for bit."""
+    from shaderintel_gb300 import _lib as L
+    d = fixture("retime.npz")
+    for case, (k, want) in enumerate(zip(d["ks"], d["out"])):
+        sim = _loaded(d, MATS_G2P, 16)
+        dt = sim.substepDt
+        if case == 0:
+            L.check(L.lib().si_mpm_set_substep_dt(sim._h, dt * 0.5))
+        elif case == 1:
+            L.check(L.lib().si_mpm_set_substep_dt(sim._h, dt * 2.0))
+        else:
+            sim.substeps = 6
+            assert np.float32(sim.substepDt / dt) == k
+        got = sim.readParticles()
+        assert np.array_equal(bits(got), bits(want)), f"k = {k}: differs from the reference's mpm-retime"
+        assert np.array_equal(bits(got), bits(O.retime(d["rec"], float(k)))), f"k = {k}: differs from the oracle"
+        sim.destroy()
+
+
+# ---------------------------------------------------------------------------- SpatialGrid (src/prims/grid.js)
+
+
+def _cells_from_order(order, start):
+    """The cell of every point, read back from a counting-sort result (order, start)."""
+    cell = np.empty(len(order), np.int64)
+    for c in np.flatnonzero(np.diff(start.astype(np.int64))):
+        cell[order[start[c]:start[c + 1]]] = c
+    return cell
+
+
+def _same_cells_as_fixture(order, start, d):
+    """Cells and starts bit-exact; the order within each cell as a set (the reference ranks points
+    in a cell by atomic arrival, so any order inside a cell is one of its outcomes)."""
+    assert np.array_equal(start, d["start"]), "start differs"
+    assert np.array_equal(_cells_from_order(order, start), d["cell"].astype(np.int64)), "cells differ"
+    for c in np.flatnonzero(np.diff(start.astype(np.int64))):
+        a, b = int(start[c]), int(start[c + 1])
+        assert sorted(order[a:b].tolist()) == sorted(d["order"][a:b].tolist()), f"cell {c} holds other points"
+
+
+def test_restatement_spatial_grid_matches_reference_wgsl():
+    import host_ref
+    d = fixture("spatial.npz")
+    cell, order, start = host_ref.spatial_grid(d["pos"], d["lo"], float(d["cell_size"]), list(d["dims"]))
+    assert np.array_equal(np.asarray(cell, np.int64), d["cell"].astype(np.int64))
+    _same_cells_as_fixture(np.asarray(order), np.asarray(start, np.uint32), d)
+    assert np.diff(d["start"].astype(np.int64)).max() >= 40          # the crowded cell
+
+
+@pytest.mark.gpu
+def test_cuda_spatial_grid_matches_reference_wgsl():
+    from shaderintel_gb300.spatial import SpatialGrid
+    d = fixture("spatial.npz")
+    g = SpatialGrid(maxCount=4096, min=list(d["lo"]), max=list(d["hi"]), cellSize=float(d["cell_size"]))
+    assert g.dims == list(d["dims"])
+    g.build(d["pos"])
+    order, start = g.read()
+    _same_cells_as_fixture(order, start, d)
+    g.destroy()
