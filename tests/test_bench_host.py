@@ -22,7 +22,7 @@ def test_reference_arm_prints_one_contract_line():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference"
-    assert d["metric"] == "MPM particle-substeps/s on 1 GB300 (plain single-scene form)"
+    assert d["metric"] == bench.METRIC and "GB300" not in d["metric"] and "n_gpus" not in d
     assert d["unit"] == "particle-substeps/s" and d["higher_is_better"] is True
     assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 3
     cb = d["cpu_baseline"]
@@ -30,6 +30,21 @@ def test_reference_arm_prints_one_contract_line():
     e = d["e2e"]
     assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
     assert d["config"]["particles"] == 32768
+    # the GPU arm's config dict, key for key: the same workload and the same frames
+    assert d["config"] == bench.run_config(bench.CONFIGS["dam_break"], 32768, 32 ** 3)
+    assert d["config"]["substeps_per_step"] == 8 and d["config"]["sort_every"] == 4
+    assert "2 frames of 8 substeps" in cb["sample"] and "after 3 warm-up frames" in cb["sample"]
+
+
+def test_summary_keys_come_first():
+    out = {"metric": "m", "value": 1.0, "unit": "u", "n_gpus": 1, "config": {}, "roofline": {},
+           "batched": {"value": 6.0, "vs_plain": 5.0, "plain_value": 1.2, "roofline": {"frac": 0.3}},
+           "served": {"value": 2.0, "p50_ms": 1.0, "p99_ms": 4.0}, "served_saturated": {"value": 4.8}}
+    s = bench.with_summary(out)
+    keys = list(s)
+    assert keys.index("batched_value") < keys.index("roofline") < keys.index("batched")
+    assert s["batched_vs_plain"] == 5.0 and s["served_p99_ms"] == 4.0
+    assert abs(s["served_saturated_vs_plain"] - 4.0) < 1e-12
 
 
 def _cells(lo, size):
