@@ -148,6 +148,7 @@ void launch_scene_starts_all(const TickInfo& t, const uint32_t* sorted_keys, uin
 cudaError_t configure_sort_kernels();
 int p2g_smem_bytes(int tile_nodes, int ppt);
 int max_tile_nodes();
-int occupancy_ctas(int which, int tile_nodes, int ppt);   // resident CTAs per SM of kernel `which`
+int occupancy_ctas(int which, int tile_nodes, int ppt);
+int couple_ctas_per_sm();                                 // resident k_couple CTAs per SM   // resident CTAs per SM of kernel `which`
 
 }  // namespace si

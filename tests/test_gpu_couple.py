@@ -89,3 +89,39 @@ def test_set_bodies_moves_the_boundary():
     imp = sim.readImpulses()
     assert not imp[:2].any()
     sim.destroy()
+
+
+def test_many_bodies_match_oracle():
+    """280 bodies: several ballot rounds of the cull, and (130 spheres piled on one spot) tiles whose
+    candidates pass the reference's 128-body cap. Particle state and every body's impulses are
+    bit-exact to the oracle."""
+    rng = np.random.default_rng(17)
+    many = np.stack([body_record(list(rng.uniform([0.2, 0.15, 0.2], [0.8, 0.45, 0.8])),
+                                 [float(rng.uniform(0.02, 0.05))] * 3, "sphere" if k % 3 else "box",
+                                 quaternion=list(rng.normal(size=4)), velocity=list(rng.uniform(-0.3, 0.3, 3)),
+                                 angular_velocity=list(rng.uniform(-1, 1, 3)), mass=float(k % 4))
+                     for k in range(150)])
+    pile = np.stack([body_record([0.5, 0.3, 0.5], [0.04] * 3, "sphere", velocity=[0, -0.1, 0], mass=1.0)
+                     for _ in range(130)])
+    allb = np.concatenate([many, pile])
+    sim = MPM(grid=24, maxParticles=120000, substeps=8)
+    sim.add({"box": [[0.15, 0.15, 0.15], [0.85, 0.45, 0.85]]}, material="water", velocity=[0.2, -0.5, 0.1])
+    sim.couple(allb, friction=0.2, band=0.5, mask=1, densityScale=1.0)
+    rec = sim.readParticles()
+    K = 6
+    sim.step(dt=sim.substepDt, K=K)
+    imp = sim.readImpulses()
+    mats = np.zeros((8, 12), np.float32)
+    mats[:len(sim._rows)] = np.stack(sim._rows)
+    dt = sim.substepDt
+    grav = [np.float32((g * dt * dt) / sim.dx) for g in sim.gravity]
+    acc = np.zeros(len(allb) * 8, np.int32)
+    cpl = {"bodies": allb, "params": [0, 0, 0, sim.dx, 1 / sim.dx, 0, dt / sim.dx, 0.2, 0.5], "mask": 1,
+           "dt": dt, "acc": acc}
+    P, _, _ = O.substeps(rec, sim.dims, mats, np.zeros((16, 12), np.float32), 0, grav, np.float32(0.5), K, 0, 4,
+                         threads=8, coupling=cpl)
+    ext, _ = O.couple_apply(acc, len(allb), np.float32(1.0 * sim.dx ** 4 / dt), sim.dx)
+    assert np.array_equal(bits(sim.readParticles()), bits(P))
+    assert np.array_equal(bits(imp), bits(ext))
+    assert imp[:, [0, 1, 2, 4, 5, 6]].any(1).sum() > 50
+    sim.destroy()
