@@ -341,8 +341,21 @@ def plasticity_specs(n, seed):
     return out
 
 
+def box_count(lo, size, edge, ppc=2):
+    """Particles add() emits for a box of `size` cells at cell `lo` of a grid of `edge` cells (size 1):
+    the lattice extent floor((hi - lo) / spacing) per axis in f64, as the emitter computes it, every
+    point kept (a box's inside test is always true)."""
+    import math
+    sp = (1.0 / edge) / ppc
+    n = 1
+    for x, d in zip(lo, size):
+        n *= max(1, math.floor(((x + d) / edge - x / edge) / sp))
+    return n
+
+
 def plasticity_capacity(s):
-    return sum(8 * (d[0] + 1) * (d[1] + 1) * (d[2] + 1) for _, _, d in s["blocks"])
+    """maxParticles of a plasticity scene: exactly the particles its two blocks emit."""
+    return sum(box_count(lo, d, s["edge"]) for _, lo, d in s["blocks"])
 
 
 def fill_plasticity(sim, s):

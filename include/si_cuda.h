@@ -275,10 +275,16 @@ typedef struct si_server_stats {
   int32_t resident_scenes, queued_requests;
 } si_server_stats;
 /* The server steps `world` from its own thread until si_server_destroy; scenes already in the
- * world become resident. Edits of resident scenes stay allowed from any thread. */
+ * world become resident. Edits of resident scenes stay allowed from any thread. Scenes created in
+ * the world while it has a server keep one particle buffer instead of two (their sort substeps read
+ * a gathered copy of the old state from the world's scratch); that scratch, and the sort's, are held
+ * below min(2 GiB, budget / 32) by running a tick's scenes in groups, and that reserve counts
+ * against the budget (si_server_stats.resident_bytes includes it). */
 int si_server_create(si_world* world, int64_t budget_bytes, si_server** out);
 int si_server_destroy(si_server* s);
-/* Admission by footprint: creates a resident scene if it fits the HBM budget, else SI_ENOMEM. */
+/* Admission by footprint: creates a resident scene if it fits the HBM budget, else SI_ENOMEM. The
+ * footprint is 128 B x maxParticles (one particle buffer) + 32 B x grid nodes + 8 B x maxParticles
+ * (block keys) + 4 B x (numBlocks + 1) + about 1.4 KB. */
 int si_server_admit(si_server* s, const si_mpm_desc* desc, si_mpm** out);
 /* Retires a scene (frees its HBM); pending requests on it complete with SI_EDESTROYED. */
 int si_server_retire(si_server* s, si_mpm* h);

@@ -35,6 +35,9 @@ constexpr uint32_t F_NO_CLEAR_NEXT = 32u; // grid update leaves grid_next alone
 constexpr uint32_t F_KEYS_NOW = 64u;  // compute the block keys of the current positions before the sort
 constexpr uint32_t F_CLEAR = 128u;    // zero `grid` before the standalone P2G
 constexpr uint32_t F_BOXED = 256u;
+constexpr uint32_t F_PREGATHER = 1024u; // with F_GATHER, a scene with one particle buffer: the read streams were
+                                        // gathered into the world's scratch in sorted order (k_pregather),
+                                        // and the G2P reads them there and writes P in place
 constexpr uint32_t F_COUPLE = 512u;   // run the fluid <-> rigid coupling pass after the grid update    // grid update: nodes outside box_cur + box_next are zero in both arrays
 
 struct SceneParams {             // per scene, device resident, rewritten when a value changes
@@ -93,6 +96,9 @@ struct TickInfo {                // one tick's totals (kernel arguments)
   uint32_t cchunks;              // 4^3 node tiles of the coupled scenes
   float nz;                      // -0.0f: the addend of packed products (see mul2z in si_kernels.cu)
   uint32_t* grid_done;           // CTAs of k_grid that finished (the last one resets it to 0)
+  const float4* gscratch;        // k_pregather's output: streams x, v, f0, f1, f2 of the sorting
+                                 // particles in sorted order (segment seg_base of each scene)
+  int64_t gstride;               // stream stride of gscratch in float4
   uint32_t* g2p_sched;           // k_g2p: [0] chunks handed out past the first wave, [1] CTAs
                                  // finished (the last one resets both to 0)
   int32_t reset_boxes;           // k_grid's last CTA empties every scene's box_next
@@ -126,8 +132,12 @@ void launch_clear(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_box_reset(const TickInfo& t, cudaStream_t st);
 void launch_couple(const TickInfo& t, int grid_ctas, cudaStream_t st);
-void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
+void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st,
+                bool pre);   // pre: the tick holds a one-buffer scene that sorts
 void launch_reorder(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
+void launch_pregather(const TickInfo& t, const uint32_t* perm, float4* scratch, int64_t stride, int grid_ctas,
+                      cudaStream_t st);
+constexpr int kPregatherStreams = 5;   // x, v (for J), f0, f1, f2: what the G2P reads of the old state
 void launch_keys(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_retime(float4* P, int64_t cap, int32_t n, float k, cudaStream_t st);
 void launch_aos_to_soa(const float* aos, float4* P, int64_t cap, int64_t off, int64_t n, cudaStream_t st);

@@ -465,6 +465,34 @@ __global__ void __launch_bounds__(kCtaThreads) k_reorder(TickInfo t, const uint3
   }
 }
 
+// The sort substep of a scene with one particle buffer: the streams its G2P reads of the old state
+// (x, v for J, and F unless the material is a fluid, whose G2P never reads F) are gathered through
+// perm into the world's scratch, segment seg_base, in sorted order. The G2P then reads them there
+// and writes the new state into P in place.
+__global__ void __launch_bounds__(kCtaThreads) k_pregather(TickInfo t, const uint32_t* __restrict__ perm,
+                                                          float4* __restrict__ scratch, int64_t stride) {
+  for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
+    const TickScene& ts = t.ts[find_scene_p(t.ts, t.nscenes, chunk)];
+    if (!(ts.flags & F_PREGATHER)) continue;
+    const int first = (int)(chunk - ts.pchunk_begin) * t.chunk;
+    const int last = min(first + t.chunk, ts.n);
+    const int64_t cap = ts.cap;
+    const SceneParams* prm = ts.prm;
+    float4* out = scratch + ts.seg_base;
+    for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+      const int64_t j = __ldg(&perm[ts.seg_base + i]);
+      const float4 x = __ldcs(&ts.P[j]);
+      out[i] = x;
+      out[stride + i] = __ldcs(&ts.P[cap + j]);
+      if (__float_as_uint(__ldg(&prm->mats[(__float_as_uint(x.w) & 7u) * 3].x)) != 0u) {
+        out[2 * stride + i] = __ldcs(&ts.P[5 * cap + j]);
+        out[3 * stride + i] = __ldcs(&ts.P[6 * cap + j]);
+        out[4 * stride + i] = __ldcs(&ts.P[7 * cap + j]);
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ grid update (mpm.js:414-471)
 __device__ __forceinline__ float collider_sdf(uint32_t kind, v3 d, float4 s) {
   if (kind == 0u) return vlen(d) - s.x;
@@ -796,7 +824,9 @@ __device__ __forceinline__ void cta_base_box(const float4 (&xs)[PPT], int count,
 
 // G2P of a chunk: gather tile (the grid nodes under the chunk's stencils, staged once in shared
 // memory), per-particle G2P, store, then the fused P2G of the next substep through the same tile.
-template <int PPT>
+// PRE: the launch may hold one-buffer scenes that sort this substep (their old state comes from the
+// pregathered scratch); ticks without one run the variant without that path.
+template <int PPT, bool PRE>
 __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t, const uint32_t* __restrict__ perm) {
   extern __shared__ __align__(16) int smem[];
   int* tile = smem;
@@ -823,10 +853,15 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
     const int first = (int)(c - ts.pchunk_begin) * chunk;
     const int count = min(chunk, ts.n - first);
     const bool fuse = (flags & F_FUSE) != 0;
-    const bool gather = (flags & F_GATHER) != 0;
-    const float4* Pin = ts.P;
+    // a sort substep reads the old state through perm and writes the other buffer, or (one-buffer
+    // scene) reads the pregathered copy in sorted order and writes its own buffer in place
+    const bool pre = PRE && (flags & F_PREGATHER) != 0;
+    const bool gather = (flags & F_GATHER) != 0 && !pre;
+    const float4* Pin = pre ? t.gscratch + ts.seg_base : ts.P;
     float4* P = gather ? ts.Palt : ts.P;
     const int64_t cap = ts.cap;
+    const int64_t cin = pre ? t.gstride : cap;             // stream stride of Pin
+    const int64_t fin = pre ? 2 * t.gstride : 5 * cap;     // offset of Pin's f0 stream
     const float4* grid = reinterpret_cast<const float4*>(ts.grid);
     const int32_t dims[3] = {prm->dims[0], prm->dims[1], prm->dims[2]};
     // 1. positions and the box of the old stencils. Lanes past the end of a partial chunk work on a
@@ -868,11 +903,11 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
       // 52 bytes per particle are not loaded. A fluid's F is reset to I (mpm.js:520-525) and its input
       // F is never read, so its 48 bytes are loaded only for the other models.
       float4 x = xs[k];
-      float4 v = make_float4(0.0f, 0.0f, 0.0f, __ldcs(reinterpret_cast<const float*>(&Pin[cap + j]) + 3));
+      float4 v = make_float4(0.0f, 0.0f, 0.0f, __ldcs(reinterpret_cast<const float*>(&Pin[cin + j]) + 3));
       float4 c0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c1 = c0, c2 = c0;
       float4 f0 = c0, f1 = c0, f2 = c0;
       if (__float_as_uint(__ldg(&prm->mats[(__float_as_uint(x.w) & 7u) * 3].x)) != 0u) {
-        f0 = __ldcs(&Pin[5 * cap + j]); f1 = __ldcs(&Pin[6 * cap + j]); f2 = __ldcs(&Pin[7 * cap + j]);
+        f0 = __ldcs(&Pin[fin + j]); f1 = __ldcs(&Pin[fin + cin + j]); f2 = __ldcs(&Pin[fin + 2 * cin + j]);
       }
       Gathered gs;
       if (gtile) gs = g2p_gather<true>(x, prm, grid, tilef, o0, o1, o2, ex, ex * ey, t.nz);
@@ -991,7 +1026,9 @@ static cudaError_t set_smem_attr(int tile_nodes) {
   if (bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_p2g<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_g2p<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    e = cudaFuncSetAttribute(k_g2p<PPT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_g2p<PPT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   }
   return cudaSuccess;
 }
@@ -1006,14 +1043,23 @@ void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st) {
     default: k_p2g<2><<<ctas, kCtaThreads, smem, st>>>(t); break;
   }
 }
-void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st) {
+void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st, bool pre) {
   if (t.pchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
   int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kCtaThreads);
   switch (t.chunk / kCtaThreads) {
-    case 1: k_g2p<1><<<ctas, kCtaThreads, smem, st>>>(t, perm); break;
-    case 4: k_g2p<4><<<ctas, kCtaThreads, smem, st>>>(t, perm); break;
-    default: k_g2p<2><<<ctas, kCtaThreads, smem, st>>>(t, perm); break;
+    case 1:
+      if (pre) k_g2p<1, true><<<ctas, kCtaThreads, smem, st>>>(t, perm);
+      else k_g2p<1, false><<<ctas, kCtaThreads, smem, st>>>(t, perm);
+      break;
+    case 4:
+      if (pre) k_g2p<4, true><<<ctas, kCtaThreads, smem, st>>>(t, perm);
+      else k_g2p<4, false><<<ctas, kCtaThreads, smem, st>>>(t, perm);
+      break;
+    default:
+      if (pre) k_g2p<2, true><<<ctas, kCtaThreads, smem, st>>>(t, perm);
+      else k_g2p<2, false><<<ctas, kCtaThreads, smem, st>>>(t, perm);
+      break;
   }
 }
 void launch_clear(const TickInfo& t, int grid_ctas, cudaStream_t st) {
@@ -1025,6 +1071,12 @@ void launch_reorder(const TickInfo& t, const uint32_t* perm, int grid_ctas, cuda
   if (t.pchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
   k_reorder<<<ctas, kCtaThreads, 0, st>>>(t, perm);
+}
+void launch_pregather(const TickInfo& t, const uint32_t* perm, float4* scratch, int64_t stride, int grid_ctas,
+                      cudaStream_t st) {
+  if (t.pchunks == 0) return;
+  int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
+  k_pregather<<<ctas, kCtaThreads, 0, st>>>(t, perm, scratch, stride);
 }
 void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st) {
   if (t.nchunks == 0) return;
@@ -1088,10 +1140,10 @@ int occupancy_ctas(int which, int tile_nodes, int ppt) {
       else if (ppt == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<4>, kCtaThreads, smem);
       else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<2>, kCtaThreads, smem);
       break;
-    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<2>, kCtaThreads, smem); break;
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<2, false>, kCtaThreads, smem); break;
     case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_grid, kCtaThreads, 0); break;
-    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<1>, kCtaThreads, smem); break;
-    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<4>, kCtaThreads, smem); break;
+    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<1, false>, kCtaThreads, smem); break;
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<4, false>, kCtaThreads, smem); break;
     default: break;
   }
   return n > 0 ? n : 1;

@@ -61,12 +61,14 @@ static uint32_t num_blocks_for(const int32_t d[3]) {
   return bpow * bpow * bpow;
 }
 
-static int64_t scene_footprint(int64_t cap, int64_t nodes, uint32_t nb) {
-  return 2 * (int64_t)kStreams * 16 * cap + 2 * 16 * nodes + 2 * 4 * cap + 4 * ((int64_t)nb + 1) +
+// Device bytes of a scene: particle buffers (two, or one for a compact scene), two grids, two key
+// buffers, the starts, the parameters and the boxes.
+static int64_t scene_footprint(int64_t cap, int64_t nodes, uint32_t nb, bool compact) {
+  return (compact ? 1 : 2) * (int64_t)kStreams * 16 * cap + 2 * 16 * nodes + 2 * 4 * cap + 4 * ((int64_t)nb + 1) +
          (int64_t)sizeof(SceneParams) + 64;
 }
 
-int64_t scene_footprint_of(const si_mpm_desc* in) {
+int64_t scene_footprint_of(const si_mpm_desc* in, bool compact) {
   si_mpm_desc d;
   si_mpm_desc_default(&d);
   if (in) {
@@ -78,7 +80,7 @@ int64_t scene_footprint_of(const si_mpm_desc* in) {
   double dx = std::max(d.size[0], std::max(d.size[1], d.size[2])) / d.grid;
   int32_t dims[3];
   for (int a = 0; a < 3; a++) dims[a] = (int32_t)std::max(8.0, js_round(d.size[a] / dx));
-  return scene_footprint(d.max_particles, (int64_t)dims[0] * dims[1] * dims[2], num_blocks_for(dims));
+  return scene_footprint(d.max_particles, (int64_t)dims[0] * dims[1] * dims[2], num_blocks_for(dims), compact);
 }
 
 void si_scene_geometry(const si_mpm* h, si_scene_geom* g) {
@@ -246,7 +248,7 @@ struct HostTick {
   std::vector<uint32_t> nb, nck, nct;   // per entry: num_blocks, node chunks, coupling tiles (host side)
   std::vector<int64_t> nodes;           // per entry: grid nodes
   uint32_t pchunks = 0, nchunks = 0, cchunks = 0;
-  bool any_p2g = false, any_clear = false, any_gather = false, any_keys_now = false;
+  bool any_p2g = false, any_clear = false, any_gather = false, any_keys_now = false, any_pregather = false;
   uint32_t sort_n = 0, sort_bins = 0, max_blocks = 0;
   int passes = 0;
 };
@@ -256,7 +258,7 @@ static TickScene base_entry(si_mpm* h) {
   std::memset(&t, 0, sizeof(t));
   t.prm = h->prm;
   t.P = h->pbuf[h->pcur];
-  t.Palt = h->pbuf[1 - h->pcur];
+  t.Palt = h->compact ? h->pbuf[0] : h->pbuf[1 - h->pcur];
   t.keys = h->keys[h->kpend];
   t.keys_next = h->keys[h->kpend];
   t.starts = h->starts;
@@ -291,6 +293,7 @@ static void finish_tick(si_world* w, HostTick& k) {
     if (t.flags & F_P2G) k.any_p2g = true;
     if (t.flags & F_CLEAR) k.any_clear = true;
     if (t.flags & F_KEYS_NOW) k.any_keys_now = true;
+    if (t.flags & F_PREGATHER) k.any_pregather = true;
     if (t.flags & F_GATHER) {
       k.any_gather = true;
       t.seg_base = seg;
@@ -329,7 +332,7 @@ static TickScene substep_entry(si_mpm* h) {
   uint32_t f = F_FUSE;
   if (h->w->flush) f |= F_FORCE_GLOBAL;
   if (!h->pending) { f |= F_P2G; if (!h->next_clear) f |= F_CLEAR; }
-  if (sort_now) { f |= F_GATHER; if (!h->keys_valid) f |= F_KEYS_NOW; }
+  if (sort_now) { f |= F_GATHER; if (!h->keys_valid) f |= F_KEYS_NOW; if (h->compact) f |= F_PREGATHER; }
   if (next_sort) f |= F_KEYS;
   if (sort_now) t.keys_next = h->keys[1 - h->kpend];   // the sort consumes keys[kpend]
   // both boxes are exact once two standard substeps ran in a row: box_cur from the P2G that filled
@@ -344,7 +347,7 @@ static TickScene substep_entry(si_mpm* h) {
   t.flags = f;
   // state after the substep
   h->gcur = 1 - h->gcur;
-  if (sort_now) { h->pcur = 1 - h->pcur; h->kpend = 1 - h->kpend; }
+  if (sort_now) { if (!h->compact) h->pcur = 1 - h->pcur; h->kpend = 1 - h->kpend; }
   h->pending = true;
   h->next_clear = false;
   h->keys_valid = next_sort;
@@ -396,6 +399,7 @@ static int64_t tick_kernels(const HostTick& k) {
     n += small_sort_ok(k.sort_n, k.sort_bins, single_sort_scene(k) != nullptr)
              ? 1 + (k.mode == T_SORT ? 1 : 0)
              : (single_sort_scene(k) ? 1 : 2) + 3 * k.passes + (k.mode == T_SORT ? 1 : 0);
+  if (k.any_pregather) n++;
   if (k.any_clear) n++;
   if (k.any_p2g) n++;
   if ((k.mode == T_SUBSTEP || k.mode == T_GRID) && k.nchunks) n++;
@@ -417,6 +421,8 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   t.nz = -0.0f;
   t.grid_done = w->grid_done;
   t.g2p_sched = w->grid_done + 1;
+  t.gscratch = w->gscratch;
+  t.gstride = (int64_t)w->gscratch_cap;
   t.reset_boxes = (k.mode == T_SUBSTEP && k.nchunks > 0) ? 1 : 0;   // else k_box_reset below
   cudaStream_t st = w->st;
   if (profile) cudaEventRecord(w->pev[0], st);
@@ -433,6 +439,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
     s.starts_out = only ? only->starts : nullptr;
     if (!launch_sort(t, s, &perm, &skeys, w->ctas_misc, st)) launch_scene_starts_all(t, skeys, k.max_blocks, st);
     if (k.mode == T_SORT) launch_reorder(t, perm, w->ctas_misc, st);
+    if (k.any_pregather) launch_pregather(t, perm, w->gscratch, (int64_t)w->gscratch_cap, w->ctas_misc, st);
   }
   if (profile) cudaEventRecord(w->pev[1], st);
   if (k.any_clear) launch_clear(t, w->ctas_grid, st);
@@ -442,7 +449,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   if (k.cchunks) launch_couple(t, w->ctas_couple, st);
   if (k.mode == T_SUBSTEP && !t.reset_boxes) launch_box_reset(t, st);   // box_next starts empty for the fused P2G
   if (profile) cudaEventRecord(w->pev[3], st);
-  if (k.mode == T_SUBSTEP || k.mode == T_G2P) launch_g2p(t, perm, w->ctas_g2p, st);
+  if (k.mode == T_SUBSTEP || k.mode == T_G2P) launch_g2p(t, perm, w->ctas_g2p, st, k.any_pregather);
   if (profile) {
     cudaEventRecord(w->pev[4], st);
     cudaEventSynchronize(w->pev[4]);
@@ -477,10 +484,21 @@ static bool same_plan(const GraphPlan& g, const std::vector<HostTick>& plan, con
 
 static int run_plan(si_world* w, std::vector<HostTick>& plan) {
   if (plan.empty()) return SI_OK;
-  uint32_t max_sort = 0;
-  for (const HostTick& k : plan) max_sort = std::max(max_sort, k.sort_n);
+  uint32_t max_sort = 0, max_pre = 0;
+  for (const HostTick& k : plan) {
+    max_sort = std::max(max_sort, k.sort_n);
+    if (k.any_pregather) max_pre = std::max(max_pre, k.sort_n);
+  }
   int r = ensure_sort_scratch(w, max_sort);
   if (r) return r;
+  if (max_pre > w->gscratch_cap) {   // the pregather scratch, grown like the sort's (graphs hold its address)
+    if (w->gscratch) CK(cudaFreeAsync(w->gscratch, w->st));
+    w->gscratch = nullptr;
+    const size_t cap = std::max<size_t>(max_pre, w->gscratch_cap + w->gscratch_cap / 2);
+    CK(cudaMallocAsync((void**)&w->gscratch, cap * 16 * kPregatherStreams, w->st));
+    w->gscratch_cap = cap;
+    world_free_graphs(w);
+  }
   std::vector<uint8_t> bytes(table_bytes(plan));
   {
     size_t off = 0;
@@ -585,9 +603,24 @@ int run_substeps(si_world* w, const std::vector<si_mpm*>& scenes, int K) {
   std::vector<HostTick> plan;
   plan.reserve(K);
   for (int s = 0; s < K; s++) {
+    // Scenes are independent, so a tick may run as several groups of scenes, one after another. A
+    // compact world splits a tick whose sorting particles exceed group_particles, which bounds the
+    // sort and pregather scratch; every scene's substep is the same in any group.
     HostTick k;
     k.mode = T_SUBSTEP;
-    for (si_mpm* h : act) push_entry(k, h, substep_entry(h));
+    int64_t sorting = 0;
+    for (si_mpm* h : act) {
+      const bool sorts = h->sort_every > 0 && h->step_count % h->sort_every == 0;
+      if (sorts && w->group_particles > 0 && sorting > 0 && sorting + h->count > w->group_particles) {
+        finish_tick(w, k);
+        plan.push_back(std::move(k));
+        k = HostTick();
+        k.mode = T_SUBSTEP;
+        sorting = 0;
+      }
+      if (sorts) sorting += h->count;
+      push_entry(k, h, substep_entry(h));
+    }
     finish_tick(w, k);
     plan.push_back(std::move(k));
   }
@@ -614,6 +647,11 @@ static int run_phase(si_mpm* h, int mode, uint32_t extra_flags) {
     case T_G2P: t.flags = 0; break;
     case T_SORT: t.flags = F_GATHER | (h->keys_valid ? 0u : F_KEYS_NOW); break;
   }
+  float4* fresh = nullptr;   // a compact scene's explicit sort reorders into a new buffer, then frees the old
+  if (mode == T_SORT && h->compact) {
+    CK(cudaMallocAsync((void**)&fresh, std::max<size_t>((size_t)kStreams * 16 * (size_t)h->cap, 16), w->st));
+    t.Palt = fresh;
+  }
   push_entry(k, h, t);
   finish_tick(w, k);
   std::vector<HostTick> plan;
@@ -622,9 +660,21 @@ static int run_phase(si_mpm* h, int mode, uint32_t extra_flags) {
   w->use_graphs = false;   // one-off phases are not worth a graph
   r = run_plan(w, plan);
   w->use_graphs = g;
-  if (r) return r;
+  if (r) {
+    if (fresh) cudaFreeAsync(fresh, w->st);
+    return r;
+  }
   if (mode == T_G2P) invalidate(h);
-  if (mode == T_SORT) { h->pcur = 1 - h->pcur; h->kpend = 1 - h->kpend; h->keys_valid = false; }
+  if (mode == T_SORT) {
+    if (h->compact) {
+      CK(cudaFreeAsync(h->pbuf[0], w->st));
+      h->pbuf[0] = fresh;
+    } else {
+      h->pcur = 1 - h->pcur;
+    }
+    h->kpend = 1 - h->kpend;
+    h->keys_valid = false;
+  }
   return SI_OK;
 }
 
@@ -689,7 +739,7 @@ int si_world_destroy(si_world* w) {
   for (si_mpm* h : sc) scene_release(h);
   world_free_graphs(w);
   for (void* p : {(void*)w->ka, (void*)w->va, (void*)w->kb, (void*)w->vb, (void*)w->hist, (void*)w->digit_total,
-                  (void*)w->tab, (void*)w->grid_done})
+                  (void*)w->tab, (void*)w->grid_done, (void*)w->gscratch})
     if (p) cudaFreeAsync(p, w->st);
   cudaStreamSynchronize(w->st);
   for (auto& e : w->pev) if (e) cudaEventDestroy(e);
@@ -828,11 +878,13 @@ int scene_create(si_world* w, const si_mpm_desc* in, si_mpm** out, bool own_worl
   h->nodes = (int64_t)h->dims[0] * h->dims[1] * h->dims[2];
   if (h->nodes * 4 > 0x7fffffffLL) { delete h; return si_fail(SI_EINVAL, "grid too large"); }
   h->num_blocks = num_blocks_for(h->dims);
-  h->device_bytes = scene_footprint(h->cap, h->nodes, h->num_blocks);
+  h->compact = w->compact;
+  h->device_bytes = scene_footprint(h->cap, h->nodes, h->num_blocks, h->compact);
   cudaStream_t st = w->st;
   const size_t pbytes = (size_t)kStreams * 16 * (size_t)h->cap;
   cudaError_t e = cudaSuccess;
-  for (int b = 0; b < 2 && e == cudaSuccess; b++) e = cudaMallocAsync((void**)&h->pbuf[b], std::max<size_t>(pbytes, 16), st);
+  for (int b = 0; b < (h->compact ? 1 : 2) && e == cudaSuccess; b++)
+    e = cudaMallocAsync((void**)&h->pbuf[b], std::max<size_t>(pbytes, 16), st);
   for (int b = 0; b < 2 && e == cudaSuccess; b++) e = cudaMallocAsync((void**)&h->grid[b], (size_t)h->nodes * 16, st);
   for (int b = 0; b < 2 && e == cudaSuccess; b++)
     e = cudaMallocAsync((void**)&h->keys[b], std::max<size_t>(4 * (size_t)h->cap, 16), st);

@@ -51,6 +51,14 @@ struct si_world {
   uint32_t* hist = nullptr;
   size_t hist_cap = 0;
   uint32_t* digit_total = nullptr;
+  // One-buffer scenes (created while `compact` is set, as a server's are): their sort substeps
+  // gather the G2P's inputs into this scratch (kPregatherStreams x 16 B per sorting particle), and a
+  // tick whose sorting particles exceed group_particles runs as several groups of scenes, so the
+  // scratch (with the sort's) stays below group_particles x 96 B.
+  bool compact = false;
+  int64_t group_particles = 0;      // 0: no limit
+  float4* gscratch = nullptr;
+  size_t gscratch_cap = 0;          // particles
   uint32_t* grid_done = nullptr;    // k_grid's finished-CTA counter, then k_g2p's chunk and finished-CTA
                                     // counters (all zero between launches)
   // tick tables of direct (non-graph) execution
@@ -103,7 +111,8 @@ struct si_mpm {
   float cols[192] = {};
   int32_t ncol = 0;
   // device state
-  float4* pbuf[2] = {nullptr, nullptr};
+  float4* pbuf[2] = {nullptr, nullptr};   // pbuf[1] is null for a one-buffer (compact) scene
+  bool compact = false;
   int pcur = 0;
   int4* grid[2] = {nullptr, nullptr};
   int gcur = 0;                     // grid of the last substep
@@ -132,7 +141,8 @@ struct si_mpm {
 int world_configure(si_world* w, int ppt, int tile_nodes);
 int run_substeps(si_world* w, const std::vector<si_mpm*>& scenes, int K);
 int scene_create(si_world* w, const si_mpm_desc* in, si_mpm** out, bool own_world);
-int64_t scene_footprint_of(const si_mpm_desc* in);
+int64_t scene_footprint_of(const si_mpm_desc* in, bool compact);
+constexpr int64_t kGroupBytesPerParticle = 16 + 16 * si::kPregatherStreams;   // sort + pregather scratch
 
 namespace si {
 cudaError_t configure_kernels(int tile_nodes);   // per device, with it current

@@ -53,7 +53,8 @@ struct Completion {              // handed to the stream callback
 
 struct si_server {
   si_world* w = nullptr;
-  int64_t budget = 0, resident = 0;
+  int64_t budget = 0, resident = 0;   // resident: scene footprints + the scratch reserve
+  int64_t reserve = 0;
   std::thread th;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -208,6 +209,12 @@ int si_server_create(si_world* w, int64_t budget_bytes, si_server** out) {
   s->w = w;
   s->budget = budget_bytes;
   std::lock_guard<std::recursive_mutex> wg(w->api_mu);
+  // Scenes admitted from now on keep one particle buffer (compact); their sort substeps use the
+  // world's sort and pregather scratch, which grouping keeps below this reserve, taken from the budget.
+  s->reserve = std::min<int64_t>(2ll << 30, budget_bytes / 32);
+  s->resident = s->reserve;
+  w->compact = true;
+  w->group_particles = std::max<int64_t>(1, s->reserve / kGroupBytesPerParticle);
   for (si_mpm* h : w->scenes) {   // scenes already in the world become resident
     h->served = true;
     s->footprint[h] = h->device_bytes;
@@ -239,6 +246,8 @@ int si_server_destroy(si_server* s) {
     std::lock_guard<std::recursive_mutex> wg(s->w->api_mu);
     for (si_mpm* h : s->w->scenes) h->served = false;
     s->w->server = nullptr;
+    s->w->compact = false;
+    s->w->group_particles = 0;
   }
   for (auto& kv : s->reqs) delete kv.second;
   delete s;
@@ -250,7 +259,7 @@ struct AdmitCtx { si_server* s; const si_mpm_desc* d; si_mpm* out; int rc; int64
 int si_server_admit(si_server* s, const si_mpm_desc* desc, si_mpm** out) {
   if (!s || !out) return si_fail(SI_EINVAL, "null argument");
   *out = nullptr;
-  const int64_t fp = scene_footprint_of(desc);
+  const int64_t fp = scene_footprint_of(desc, true);
   {
     std::lock_guard<std::mutex> g(s->mu);
     if (s->resident + fp > s->budget)

@@ -52,8 +52,12 @@ def alone(spec, plan):
     return out
 
 
-def test_served_results_equal_alone():
-    srv = Server(budget_bytes=4 * 10 ** 9)
+@pytest.mark.parametrize("budget", [4 * 10 ** 9, 6 * 10 ** 7])
+def test_served_results_equal_alone(budget):
+    """Served scenes keep one particle buffer (their sort substeps read a gathered copy of the old
+    state). With the small budget the sort scratch reserve (budget / 32) holds about 20,000 particles,
+    so a tick whose scenes sort together runs as several groups of scenes: the bits do not change."""
+    srv = Server(budget_bytes=budget)
     sims = [fill(srv.admit(grid=s[0], maxParticles=cap_of(s), substeps=8), s) for s in SCENES]
     dt0 = sims[0].substepDt
     rng = random.Random(5)
@@ -93,12 +97,16 @@ def test_served_results_equal_alone():
 
 def test_admission_by_footprint_and_retire():
     one = Server(budget_bytes=10 ** 12)
+    reserve = one.stats()["resident_bytes"]        # the sort scratch reserve: min(2 GiB, budget / 32)
+    assert reserve == min(2 << 30, 10 ** 12 // 32)
     probe = one.admit(grid=32, maxParticles=100000)
-    fp = one.stats()["resident_bytes"]
+    fp = one.stats()["resident_bytes"] - reserve
     one.destroy()
-    assert fp > 100000 * 256
+    # one particle buffer (128 B a particle), two grids, two key buffers: not two particle buffers
+    assert 100000 * 136 + 32 ** 3 * 32 <= fp < 100000 * 256
 
-    srv = Server(budget_bytes=int(fp * 1.5))
+    budget = int(fp * 1.5 * 32 / 31)               # a reserve of budget / 32 leaves room for 1.5 scenes
+    srv = Server(budget_bytes=budget)
     a = srv.admit(grid=32, maxParticles=100000)
     with pytest.raises(SIError) as e:
         srv.admit(grid=32, maxParticles=100000)
@@ -186,3 +194,20 @@ def test_queued_requests_keep_their_own_colliders():
         free.step(dt=dt, K=K)
     assert not np.array_equal(bits(free.readParticles()), bits(want))
     free.destroy()
+
+
+def test_explicit_sort_of_a_served_scene():
+    """_sort() of a one-buffer scene reorders into a fresh buffer; the records equal those of the
+    same scene with two buffers."""
+    srv = Server(budget_bytes=4 * 10 ** 9)
+    spec = SCENES[3]
+    a = fill(srv.admit(grid=spec[0], maxParticles=cap_of(spec), substeps=8), spec)
+    assert srv.wait(srv.submit(a, K=5), timeout_ms=60000) == 0
+    b = fill(MPM(None, grid=spec[0], maxParticles=cap_of(spec), substeps=8), spec)
+    b.step(dt=b.substepDt, K=5)
+    a._sort()                                  # between rounds: the world's lock serialises it
+    b._sort()
+    assert np.array_equal(bits(a.readParticles()), bits(b.readParticles()))
+    assert all(np.array_equal(x, y) for x, y in zip(a.readBins(), b.readBins()))
+    srv.destroy()
+    b.destroy()
