@@ -716,6 +716,14 @@ def with_summary(out):
         summ["served_saturated_value"] = ss["value"]
         if b:   # the plain aggregate of scenes drawn from the same distribution, stepped one by one
             summ["served_saturated_vs_plain"] = ss["value"] / b["plain_value"]
+    spl = out.get("served_plasticity") or []
+    if spl:
+        summ["served_plasticity_resident_scenes"] = spl[0]["resident_scenes"]
+        summ["served_plasticity_capacity"] = spl[0]["value"]
+        if len(spl) > 1:   # the run at the rate the GPU sustains
+            summ["served_plasticity_sustained_rate_per_s"] = spl[1].get("rate_per_s")
+            summ["served_plasticity_sustained_p50_ms"] = spl[1]["p50_ms"]
+            summ["served_plasticity_sustained_p99_ms"] = spl[1]["p99_ms"]
     head = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
             "vs_baseline", "dtype", "data", "config")
     first = {k: out[k] for k in head if k in out}
@@ -758,8 +766,9 @@ def main():
                    help="skip the served leg over 1 M-particle plasticity scenes")
     p.add_argument("--serve-p-seconds", type=float, default=2.0,
                    help="arrival window of each served-plasticity run (every request is then waited for)")
-    p.add_argument("--serve-p-rates", default="2000,200",
-                   help="arrival rates (requests/s) of the served-plasticity runs")
+    p.add_argument("--serve-p-rates", default="2000,sustain,200",
+                   help="arrival rates (requests/s) of the served-plasticity runs; 'sustain' = 85 %% of the "
+                        "capacity the previous run measured, in requests of mean K over the mean resident scene")
     p.add_argument("--only-batched", action="store_true",
                    help="run the batched leg alone (its line carries the batched metric), e.g. under a profiler")
     p.add_argument("--no-autotune", action="store_true", help="batched leg with the default tuning")
@@ -795,9 +804,18 @@ def main():
     if world_size == 1 and not a.no_served and not a.no_served_plasticity:
         import types
         out["served_plasticity"] = []
-        for rate in (float(x) for x in a.serve_p_rates.split(",") if x):
+        for tok in (x for x in a.serve_p_rates.split(",") if x):
+            if tok == "sustain":
+                prev = out["served_plasticity"][-1] if out["served_plasticity"] else None
+                if not prev:
+                    continue
+                per_request = 16.5 * prev["resident_particles"] / max(1, prev["resident_scenes"])   # K uniform 1..32
+                rate = round(0.85 * prev["value"] / per_request)
+            else:
+                rate = float(tok)
             sp = types.SimpleNamespace(serve_rate=rate, serve_seconds=a.serve_p_seconds, serve_resident=1000)
             out["served_plasticity"].append(run_served(sp, log, scenes="plasticity"))
+            out["served_plasticity"][-1]["rate_per_s"] = rate
     if world_size == 1:
         out["conservation"] = run_conservation()
         out["extras"] = run_extras()
