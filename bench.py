@@ -371,17 +371,24 @@ def b_alg(sims):
     return sum(256 * s.count + 32 * s.numNodes for s in sims)
 
 
-def run_batched(a, log):
+SVD_TOL = "snow and sand decompose F to a tolerance (si_world_set_svd_tolerance): particle x, v, C, F, J " \
+          "within 1e-5 relative per substep of the bit-exact path, binning and grid sums exact"
+
+
+def run_batched(a, log, svd_tol=True, tune=None):
     """256 scenes in one world: one launch per phase for all of them, CUDA graphs, autotuned; against
     the same scenes each stepped alone (the plain single-scene path) one after another."""
     from shaderintel_gb300 import MPM, World
     from shaderintel_gb300.autotune import autotune
     specs = scene_specs(a.batch_scenes, 4242)
     world = World()
+    world.set_svd_tolerance(svd_tol)
     sims = [fill_scene(MPM(world, grid=s["edge"], maxParticles=spec_capacity(s), substeps=8), s) for s in specs]
     n_total = sum(s.count for s in sims)
     K = a.batch_substeps
-    if a.no_autotune:
+    if tune is not None:
+        world.set_tuning(tune["particles_per_cta"], tune["tile_nodes"], tune["flush"])
+    elif a.no_autotune:
         tune = {"particles_per_cta": 256, "tile_nodes": 2048, "flush": 0, "autotuned": False}
     else:
         tune = autotune(world, substeps=4, repeats=2)
@@ -423,6 +430,7 @@ def run_batched(a, log):
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "peak_source": peak_kind, "algorithmic_bytes_per_substep": bytes_substep},
            "tuning": tune, "gpu_launches": launches, "clocks": clk,
+           "svd": SVD_TOL if svd_tol else "bit-exact",
            "l2": f"inputs larger than L2 ({n_total * 128 / 1e6:.0f} MB particle state)"}
     world.destroy()
     return out
@@ -448,6 +456,7 @@ def run_served(a, log, scenes="batched"):
         cap_of, fill_of = spec_capacity, fill_scene
         drawn = "the batched workload"
     srv = Server(budget_bytes=150 * 10 ** 9)
+    srv.world.set_svd_tolerance(True)
     peak, _ = load_peaks()
     resident, given, size_of, outstanding = [], {}, {}, collections.defaultdict(list)
     retiring = []
@@ -538,7 +547,7 @@ def run_served(a, log, scenes="batched"):
             "admitted": admitted, "retired": retired, "refused": refused,
             "roofline": {"bound": "hbm", "achieved": bytes_done / wall / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": bytes_done / wall / 1e9 / peak},
-            "resident_peak_bytes": st["resident_bytes"], "budget_bytes": st["budget_bytes"]}
+            "resident_peak_bytes": st["resident_bytes"], "budget_bytes": st["budget_bytes"], "svd": SVD_TOL}
 
 
 def run_conservation(substeps=200):
@@ -706,6 +715,10 @@ def with_summary(out):
         summ["batched_value"] = b["value"]
         summ["batched_vs_plain"] = b["vs_plain"]
         summ["batched_roofline_frac"] = b["roofline"]["frac"]
+        if "bit_exact" in b:
+            summ["batched_bit_exact_value"] = b["bit_exact"]["value"]
+            summ["batched_bit_exact_vs_plain"] = b["bit_exact"]["vs_plain"]
+            summ["batched_bit_exact_roofline_frac"] = b["bit_exact"]["roofline_frac"]
     sv = out.get("served")
     if sv:
         summ["served_value"] = sv["value"]
@@ -794,6 +807,10 @@ def main():
     log = lambda m: print(m, file=sys.stderr, flush=True)   # noqa: E731
     if world_size == 1 and not a.no_batched:
         out["batched"] = run_batched(a, log)
+        # the same leg with every field bit-identical to the CPU restatement, beside it
+        ex = run_batched(a, log, svd_tol=False, tune=out["batched"]["tuning"])
+        out["batched"]["bit_exact"] = {k: ex[k] for k in ("value", "plain_value", "vs_plain", "ms_per_step")}
+        out["batched"]["bit_exact"]["roofline_frac"] = ex["roofline"]["frac"]
     if world_size == 1 and not a.no_served:
         out["served"] = run_served(a, log)
         # the same loop offered more than it can run: its capacity (latency is then queueing)

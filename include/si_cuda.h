@@ -82,6 +82,13 @@ int si_world_destroy(si_world* w);                  /* destroys its scenes too; 
 int si_world_step(si_world* w, int32_t K);          /* K substeps of every scene, each at its own dt */
 int si_world_sync(si_world* w);
 int si_world_set_graphs(si_world* w, int32_t enable); /* replay substeps from CUDA graphs (default 1) */
+/* Snow and sand decompose F (svd3 of linalg.js:46-69: four Jacobi sweeps on F^T F) to a tolerance
+ * instead of bit for bit: fused multiply-adds and the hardware reciprocal square root in place of
+ * IEEE division and square root. Particle x, v, C, F and J stay within 1e-5 relative of the exact
+ * path per substep from the same state; grid sums and binning remain exact integers of that state.
+ * Default 0 (every field bit-identical to the CPU restatement of the reference). Worlds only; no
+ * counterpart in the reference (its WGSL leaves the rounding of these operations open). */
+int si_world_set_svd_tolerance(si_world* w, int32_t enable);
 /* Per-phase GPU time in ms since the last reset: [sort, p2g, grid, g2p] — the labels
  * 'mpm sort' | 'mpm p2g' | 'mpm grid' | 'mpm g2p' of mpm.js:591-600. Timing is off until enabled. */
 int si_world_profile(si_world* w, int32_t enable, double ms_out[4], int32_t reset);

@@ -55,6 +55,7 @@ SIGNATURES = {
     "si_world_step": (ctypes.c_int, [vp, ctypes.c_int32]),
     "si_world_sync": (ctypes.c_int, [vp]),
     "si_world_set_graphs": (ctypes.c_int, [vp, ctypes.c_int32]),
+    "si_world_set_svd_tolerance": (ctypes.c_int, [vp, ctypes.c_int32]),
     "si_world_profile": (ctypes.c_int, [vp, ctypes.c_int32, c_double_p, ctypes.c_int32]),
     "si_world_set_tuning": (ctypes.c_int, [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "si_world_mark": (ctypes.c_int, [vp, ctypes.c_int32]),

@@ -19,7 +19,11 @@
 namespace si {
 
 constexpr int kStreams = 8;           // float4 streams per particle
-constexpr int kCtaThreads = 256;      // threads per CTA of the particle kernels
+constexpr int kCtaThreads = 256;      // threads per CTA of the streaming kernels (sort, grid, copies)
+#ifndef SI_CHUNK_THREADS
+#define SI_CHUNK_THREADS 256
+#endif
+constexpr int kChunkThreads = SI_CHUNK_THREADS;   // threads per CTA of the P2G/G2P kernels (particles per chunk / ppt)
 constexpr int kMaxPpt = 4;            // particles per thread in one chunk, at most
 constexpr int kNodeChunk = 2048;      // grid nodes per work item of the grid kernel (small grids: fewer)
 constexpr int kSortTile = 4096;       // keys per CTA of a radix pass (256 threads x 16)
@@ -133,7 +137,8 @@ void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_box_reset(const TickInfo& t, cudaStream_t st);
 void launch_couple(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st,
-                bool pre);   // pre: the tick holds a one-buffer scene that sorts
+                bool pre,     // the tick holds a one-buffer scene that sorts
+                bool fast);   // snow and sand decompose F to a tolerance
 void launch_reorder(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st);
 void launch_pregather(const TickInfo& t, const uint32_t* perm, float4* scratch, int64_t stride, int grid_ctas,
                       cudaStream_t st);

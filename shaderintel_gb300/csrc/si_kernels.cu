@@ -262,11 +262,11 @@ template <typename Fn>
 __device__ __forceinline__ void tile_walk(int ex, int ey, int ez, Fn&& f) {
   const int tid = threadIdx.x;
   const int exy = ex * ey;
-  const bool narrow = exy < kCtaThreads;
-  const int zs = narrow ? kCtaThreads / exy : 1;
+  const bool narrow = exy < kChunkThreads;
+  const int zs = narrow ? kChunkThreads / exy : 1;
   const int z0 = narrow ? tid / exy : 0;
   if (z0 >= zs) return;
-  for (int col = narrow ? tid - z0 * exy : tid; col < exy; col += narrow ? exy : kCtaThreads) {
+  for (int col = narrow ? tid - z0 * exy : tid; col < exy; col += narrow ? exy : kChunkThreads) {
     const int ly = col / ex, lx = col - ly * ex;
     for (int lz = z0; lz < ez; lz += zs) f(col + exy * lz, lx, ly, lz);
   }
@@ -318,7 +318,7 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
     atomicMin(&sbox[0], lo0); atomicMin(&sbox[1], lo1); atomicMin(&sbox[2], lo2);
     atomicMax(&sbox[3], hi0); atomicMax(&sbox[4], hi1); atomicMax(&sbox[5], hi2);
   }
-  if (sc == nullptr && tid == kCtaThreads / 2) { sbox[8] = reg.b[0]; sbox[9] = reg.b[1]; sbox[10] = reg.b[2]; }
+  if (sc == nullptr && tid == kChunkThreads / 2) { sbox[8] = reg.b[0]; sbox[9] = reg.b[1]; sbox[10] = reg.b[2]; }
   cta_sync();
   const int o0 = sbox[0], o1 = sbox[1], o2 = sbox[2];
   const int ex = sbox[3] - o0 + 3, ey = sbox[4] - o1 + 3, ez = sbox[5] - o2 + 3;
@@ -400,12 +400,12 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
 
 // ------------------------------------------------------------------ P2G kernel (mpm.js:306-401)
 template <int PPT>
-__global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t) {
+__global__ void __launch_bounds__(kChunkThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t) {
   extern __shared__ __align__(16) int smem[];
   int* tile = smem;
   int* sbox = smem + 4 * kTileNodes;
   float* sc = reinterpret_cast<float*>(sbox + 24);
-  constexpr int chunk = kCtaThreads * PPT;
+  constexpr int chunk = kChunkThreads * PPT;
   box_empty(sbox);
   cta_sync();
   for (uint32_t c = blockIdx.x; c < t.pchunks; c += gridDim.x) {
@@ -421,14 +421,14 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t
     Scat reg;
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-      const bool valid = k * kCtaThreads + (int)threadIdx.x < count;
-      const int64_t i = first + min(k * kCtaThreads + (int)threadIdx.x, count - 1);
+      const bool valid = k * kChunkThreads + (int)threadIdx.x < count;
+      const int64_t i = first + min(k * kChunkThreads + (int)threadIdx.x, count - 1);
       float4 x = __ldg(&src[i]), v = __ldg(&src[cap + i]);
       float4 c0 = __ldg(&src[2 * cap + i]), c1 = __ldg(&src[3 * cap + i]), c2 = __ldg(&src[4 * cap + i]);
       float t01 = __ldg(&src[5 * cap + i].w), t02 = __ldg(&src[6 * cap + i].w), t12 = __ldg(&src[7 * cap + i].w);
       prep_scatter(reg, x, v, c0, c1, c2, t01, t02, t12, prm);
       if (!valid) scat_silence(reg);
-      if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + threadIdx.x, reg);
+      if (PPT > 1) scat_store(sc, chunk, k * kChunkThreads + threadIdx.x, reg);
     }
     cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
                 reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox, nullptr,
@@ -676,7 +676,8 @@ __device__ __forceinline__ Gathered g2p_gather(const float4& X, const SceneParam
 }
 
 // C, velocity clamp, advection and the constitutive update of one particle from its gathered sums
-// (mpm.js:510-558).
+// (mpm.js:510-558). FAST: snow and sand decompose F with svd3_fast (to a tolerance) instead of svd3.
+template <bool FAST>
 __device__ __forceinline__ void g2p_update(const Gathered& g, float4& X, float4& Vv, float4& C0, float4& C1,
                                            float4& C2, float4& F0, float4& F1, float4& F2,
                                            const SceneParams* prm) {
@@ -736,7 +737,8 @@ __device__ __forceinline__ void g2p_update(const Gathered& g, float4& X, float4&
     } else {
       // snow and sand share one inlined copy of the SVD
       m3 U, Vm; v3 sv;
-      svd3(F, U, sv, Vm);
+      if (FAST) svd3_fast(F, U, sv, Vm);
+      else svd3(F, U, sv, Vm);
       if (kind == 2u) {
         const float lo_s = 1.0f - m1.z, hi_s = 1.0f + m1.w;
         const v3 s = V(clampf(sv.x, lo_s, hi_s), clampf(sv.y, lo_s, hi_s), clampf(sv.z, lo_s, hi_s));
@@ -826,15 +828,16 @@ __device__ __forceinline__ void cta_base_box(const float4 (&xs)[PPT], int count,
 // memory), per-particle G2P, store, then the fused P2G of the next substep through the same tile.
 // PRE: the launch may hold one-buffer scenes that sort this substep (their old state comes from the
 // pregathered scratch); ticks without one run the variant without that path.
-template <int PPT, bool PRE>
-__global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t, const uint32_t* __restrict__ perm) {
+// FAST: the world decomposes snow and sand to a tolerance (si_world_set_svd_tolerance).
+template <int PPT, bool PRE, bool FAST>
+__global__ void __launch_bounds__(kChunkThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t, const uint32_t* __restrict__ perm) {
   extern __shared__ __align__(16) int smem[];
   int* tile = smem;
   float4* tilef = reinterpret_cast<float4*>(smem);
   int* gbox = smem + 4 * kTileNodes;   // box of the old stencils (gather tile)
   int* sbox = gbox + 8;                // box of the new bases (scatter tile) and its middle base
   float* sc = reinterpret_cast<float*>(gbox + 24);
-  constexpr int chunk = kCtaThreads * PPT;
+  constexpr int chunk = kChunkThreads * PPT;
   const int tid = threadIdx.x;
   // Chunks are handed out in order as CTAs become free: the first wave by CTA index, the rest from a
   // counter that thread 0 bumps at the start of a chunk for the CTA's next one (chunk costs differ by
@@ -872,7 +875,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
     int64_t js[PPT];
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-      const int slot = min(k * kCtaThreads + tid, count - 1);
+      const int slot = min(k * kChunkThreads + tid, count - 1);
       js[k] = gather ? (int64_t)__ldg(&perm[ts.seg_base + first + slot]) : (int64_t)(first + slot);
       xs[k] = __ldcs(&Pin[js[k]]);
     }
@@ -896,8 +899,8 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
     Scat reg;
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-      const bool valid = k * kCtaThreads + tid < count;
-      const int slot = min(k * kCtaThreads + tid, count - 1);
+      const bool valid = k * kChunkThreads + tid < count;
+      const int slot = min(k * kChunkThreads + tid, count - 1);
       const int64_t i = first + slot, j = js[k];
       // G2P reads x, J (v.w) and F; v.xyz, C and the stress are recomputed (mpm.js:479-559), so their
       // 52 bytes per particle are not loaded. A fluid's F is reset to I (mpm.js:520-525) and its input
@@ -912,7 +915,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
       Gathered gs;
       if (gtile) gs = g2p_gather<true>(x, prm, grid, tilef, o0, o1, o2, ex, ex * ey, t.nz);
       else gs = g2p_gather<false>(x, prm, grid, tilef, 0, 0, 0, 1, 1, t.nz);
-      g2p_update(gs, x, v, c0, c1, c2, f0, f1, f2, prm);
+      g2p_update<FAST>(gs, x, v, c0, c1, c2, f0, f1, f2, prm);
       if (valid) {
         __stcs(&P[i], x); __stcs(&P[cap + i], v); __stcs(&P[2 * cap + i], c0); __stcs(&P[3 * cap + i], c1);
         __stcs(&P[4 * cap + i], c2); __stcs(&P[5 * cap + i], f0); __stcs(&P[6 * cap + i], f1);
@@ -922,7 +925,7 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
       if (fuse) {
         prep_scatter(reg, x, v, c0, c1, c2, f0.w, f1.w, f2.w, prm);
         if (!valid) scat_silence(reg);
-        if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + tid, reg);
+        if (PPT > 1) scat_store(sc, chunk, k * kChunkThreads + tid, reg);
       }
     }
     // 4. P2G of the next substep through the same shared memory; it empties both boxes for the next
@@ -1016,7 +1019,7 @@ __global__ void k_instances(const float4* __restrict__ P, int64_t cap, int64_t o
 // ------------------------------------------------------------------ launchers
 int p2g_smem_bytes(int tile_nodes, int ppt) {
   (void)tile_nodes;
-  return kTileNodes * 16 + 96 + (ppt > 1 ? kScatWords * 4 * kCtaThreads * ppt : 0);
+  return kTileNodes * 16 + 96 + (ppt > 1 ? kScatWords * 4 * kChunkThreads * ppt : 0);
 }
 int max_tile_nodes() { return kTileNodes; }
 
@@ -1026,9 +1029,11 @@ static cudaError_t set_smem_attr(int tile_nodes) {
   if (bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_p2g<PPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_g2p<PPT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_g2p<PPT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    for (const void* k : {(const void*)k_g2p<PPT, false, false>, (const void*)k_g2p<PPT, true, false>,
+                          (const void*)k_g2p<PPT, false, true>, (const void*)k_g2p<PPT, true, true>}) {
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaSuccess;
 }
@@ -1036,30 +1041,32 @@ static cudaError_t set_smem_attr(int tile_nodes) {
 void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st) {
   if (t.pchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
-  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kCtaThreads);
-  switch (t.chunk / kCtaThreads) {
-    case 1: k_p2g<1><<<ctas, kCtaThreads, smem, st>>>(t); break;
-    case 4: k_p2g<4><<<ctas, kCtaThreads, smem, st>>>(t); break;
-    default: k_p2g<2><<<ctas, kCtaThreads, smem, st>>>(t); break;
+  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kChunkThreads);
+  switch (t.chunk / kChunkThreads) {
+    case 1: k_p2g<1><<<ctas, kChunkThreads, smem, st>>>(t); break;
+    case 4: k_p2g<4><<<ctas, kChunkThreads, smem, st>>>(t); break;
+    default: k_p2g<2><<<ctas, kChunkThreads, smem, st>>>(t); break;
   }
 }
-void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st, bool pre) {
+template <int PPT>
+static void launch_g2p_ppt(const TickInfo& t, const uint32_t* perm, int ctas, int smem, cudaStream_t st, bool pre,
+                           bool fast) {
+  if (pre) {
+    if (fast) k_g2p<PPT, true, true><<<ctas, kChunkThreads, smem, st>>>(t, perm);
+    else k_g2p<PPT, true, false><<<ctas, kChunkThreads, smem, st>>>(t, perm);
+  } else {
+    if (fast) k_g2p<PPT, false, true><<<ctas, kChunkThreads, smem, st>>>(t, perm);
+    else k_g2p<PPT, false, false><<<ctas, kChunkThreads, smem, st>>>(t, perm);
+  }
+}
+void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st, bool pre, bool fast) {
   if (t.pchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
-  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kCtaThreads);
-  switch (t.chunk / kCtaThreads) {
-    case 1:
-      if (pre) k_g2p<1, true><<<ctas, kCtaThreads, smem, st>>>(t, perm);
-      else k_g2p<1, false><<<ctas, kCtaThreads, smem, st>>>(t, perm);
-      break;
-    case 4:
-      if (pre) k_g2p<4, true><<<ctas, kCtaThreads, smem, st>>>(t, perm);
-      else k_g2p<4, false><<<ctas, kCtaThreads, smem, st>>>(t, perm);
-      break;
-    default:
-      if (pre) k_g2p<2, true><<<ctas, kCtaThreads, smem, st>>>(t, perm);
-      else k_g2p<2, false><<<ctas, kCtaThreads, smem, st>>>(t, perm);
-      break;
+  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kChunkThreads);
+  switch (t.chunk / kChunkThreads) {
+    case 1: launch_g2p_ppt<1>(t, perm, ctas, smem, st, pre, fast); break;
+    case 4: launch_g2p_ppt<4>(t, perm, ctas, smem, st, pre, fast); break;
+    default: launch_g2p_ppt<2>(t, perm, ctas, smem, st, pre, fast); break;
   }
 }
 void launch_clear(const TickInfo& t, int grid_ctas, cudaStream_t st) {
@@ -1136,14 +1143,14 @@ int occupancy_ctas(int which, int tile_nodes, int ppt) {
   int smem = p2g_smem_bytes(tile_nodes, ppt);
   switch (which) {
     case 0:
-      if (ppt == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<1>, kCtaThreads, smem);
-      else if (ppt == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<4>, kCtaThreads, smem);
-      else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<2>, kCtaThreads, smem);
+      if (ppt == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<1>, kChunkThreads, smem);
+      else if (ppt == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<4>, kChunkThreads, smem);
+      else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<2>, kChunkThreads, smem);
       break;
-    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<2, false>, kCtaThreads, smem); break;
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<2, false, false>, kChunkThreads, smem); break;
     case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_grid, kCtaThreads, 0); break;
-    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<1, false>, kCtaThreads, smem); break;
-    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<4, false>, kCtaThreads, smem); break;
+    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<1, false, false>, kChunkThreads, smem); break;
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<4, false, false>, kChunkThreads, smem); break;
     default: break;
   }
   return n > 0 ? n : 1;

@@ -242,4 +242,84 @@ __device__ __forceinline__ void svd3(const m3& F, m3& U, v3& s_out, m3& Vm) {
   s_out = s;
 }
 
+// ---- svd3 to a tolerance instead of bit for bit (SI_FAST_SVD builds): the same four cyclic Jacobi
+// sweeps on F^T F, eigen sort and Gram-Schmidt U as svd3, but with fused multiply-adds and the
+// hardware reciprocal square root and fast division in place of IEEE division and square root.
+__device__ __forceinline__ void jacobi_rotate_fast_pq(m3& A, m3& Vm, int p, int q) {
+  const float apq = get(A.c[q], p);
+  if (fabsf(apq) < 1e-30f) return;
+  const float theta = __fdividef(get(A.c[q], q) - get(A.c[p], p), 2.0f * apq);
+  const float h = __fmaf_rn(theta, theta, 1.0f);
+  const float root_h = h < 1e30f ? h * rsqrtf(h) : fabsf(theta);   // sqrt(1 + theta^2), also for huge theta
+  const float t = __fdividef(theta >= 0.0f ? 1.0f : -1.0f, fabsf(theta) + root_h);
+  const float c = rsqrtf(__fmaf_rn(t, t, 1.0f));
+  const float s = t * c;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const float ap = get(A.c[j], p), aq = get(A.c[j], q);
+    put(A.c[j], p, __fmaf_rn(c, ap, -s * aq));
+    put(A.c[j], q, __fmaf_rn(s, ap, c * aq));
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float tp = get(A.c[p], i), tq = get(A.c[q], i);
+    put(A.c[p], i, __fmaf_rn(tp, c, -tq * s));
+    put(A.c[q], i, __fmaf_rn(tp, s, tq * c));
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float vp = get(Vm.c[p], i), vq = get(Vm.c[q], i);
+    put(Vm.c[p], i, __fmaf_rn(vp, c, -vq * s));
+    put(Vm.c[q], i, __fmaf_rn(vp, s, vq * c));
+  }
+}
+template <int p, int q>
+__device__ __forceinline__ void jacobi_rotate_fast(m3& A, m3& Vm) { jacobi_rotate_fast_pq(A, Vm, p, q); }
+
+__device__ __forceinline__ float dot_fma(v3 a, v3 b) { return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, a.x * b.x)); }
+__device__ __forceinline__ v3 mv_fma(const m3& m, v3 v) {
+  return V(__fmaf_rn(m.c[2].x, v.z, __fmaf_rn(m.c[1].x, v.y, m.c[0].x * v.x)),
+           __fmaf_rn(m.c[2].y, v.z, __fmaf_rn(m.c[1].y, v.y, m.c[0].y * v.x)),
+           __fmaf_rn(m.c[2].z, v.z, __fmaf_rn(m.c[1].z, v.y, m.c[0].z * v.x)));
+}
+
+__device__ __forceinline__ void svd3_fast(const m3& F, m3& U, v3& s_out, m3& Vm) {
+  m3 A;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    A.c[j] = V(dot_fma(F.c[0], F.c[j]), dot_fma(F.c[1], F.c[j]), dot_fma(F.c[2], F.c[j]));
+  }
+  Vm.c[0] = V(1.0f, 0.0f, 0.0f); Vm.c[1] = V(0.0f, 1.0f, 0.0f); Vm.c[2] = V(0.0f, 0.0f, 1.0f);
+#pragma unroll 1
+  for (int sweep = 0; sweep < 4; sweep++) {
+    jacobi_rotate_fast<0, 1>(A, Vm);
+    jacobi_rotate_fast<0, 2>(A, Vm);
+    jacobi_rotate_fast<1, 2>(A, Vm);
+  }
+  v3 e = V(A.c[0].x, A.c[1].y, A.c[2].z);
+  if (e.x < e.y) { e = V(e.y, e.x, e.z); v3 c0 = Vm.c[0]; Vm.c[0] = Vm.c[1]; Vm.c[1] = c0; Vm.c[2] = vneg(Vm.c[2]); }
+  if (e.x < e.z) { e = V(e.z, e.y, e.x); v3 c0 = Vm.c[0]; Vm.c[0] = Vm.c[2]; Vm.c[1] = vneg(Vm.c[1]); Vm.c[2] = c0; }
+  if (e.y < e.z) { e = V(e.x, e.z, e.y); v3 c1 = Vm.c[1]; Vm.c[0] = vneg(Vm.c[0]); Vm.c[1] = Vm.c[2]; Vm.c[2] = c1; }
+  if (det3(Vm) < 0.0f) Vm.c[2] = vneg(Vm.c[2]);
+  auto root = [](float x) { return x > 0.0f ? x * rsqrtf(x) : 0.0f; };
+  v3 s = V(root(e.x), root(e.y), root(e.z));
+  v3 u0 = mv_fma(F, Vm.c[0]);
+  const float q0 = dot_fma(u0, u0);
+  u0 = q0 > 1e-24f ? vscale(rsqrtf(q0), u0) : V(1.0f, 0.0f, 0.0f);
+  v3 u1 = mv_fma(F, Vm.c[1]);
+  u1 = vsub(u1, vscale(dot_fma(u1, u0), u0));
+  const float q1 = dot_fma(u1, u1);
+  if (q1 > 1e-24f) {
+    u1 = vscale(rsqrtf(q1), u1);
+  } else {
+    u1 = fabsf(u0.x) < 0.9f ? V(1.0f, 0.0f, 0.0f) : V(0.0f, 1.0f, 0.0f);
+    u1 = vsub(u1, vscale(dot_fma(u1, u0), u0));
+    u1 = vscale(rsqrtf(dot_fma(u1, u1)), u1);
+  }
+  const v3 u2 = vcross(u0, u1);
+  if (dot_fma(mv_fma(F, Vm.c[2]), u2) < 0.0f) s.z = -s.z;
+  U.c[0] = u0; U.c[1] = u1; U.c[2] = u2;
+  s_out = s;
+}
+
 }  // namespace si

@@ -66,6 +66,7 @@ struct si_world {
   size_t tab_cap = 0;
   // graphs
   bool use_graphs = true;
+  bool svd_tolerance = false;       // snow/sand SVD to a tolerance (si_world_set_svd_tolerance)
   std::vector<std::unique_ptr<GraphPlan>> graphs;
   uint64_t graph_clock = 0;
   uint64_t seen[16] = {};           // hashes of recent plans: a plan is captured when it repeats

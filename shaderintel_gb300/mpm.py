@@ -139,6 +139,11 @@ class World:
     def set_graphs(self, on):
         check(L.lib().si_world_set_graphs(self._h, 1 if on else 0))
 
+    def set_svd_tolerance(self, on):
+        """Snow and sand decompose F to a tolerance (x, v, C, F, J within 1e-5 relative per substep of
+        the bit-exact path) instead of bit for bit: faster plasticity. Off by default."""
+        check(L.lib().si_world_set_svd_tolerance(self._h, 1 if on else 0))
+
     def profile(self, enable=True, reset=False):
         """Per-phase GPU ms {'mpm sort', 'mpm p2g', 'mpm grid', 'mpm g2p'} (labels of mpm.js:591-600)."""
         ms = (ctypes.c_double * 4)()
