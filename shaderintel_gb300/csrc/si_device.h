@@ -19,11 +19,7 @@
 namespace si {
 
 constexpr int kStreams = 8;           // float4 streams per particle
-constexpr int kCtaThreads = 256;      // threads per CTA of the streaming kernels (sort, grid, copies)
-#ifndef SI_CHUNK_THREADS
-#define SI_CHUNK_THREADS 256
-#endif
-constexpr int kChunkThreads = SI_CHUNK_THREADS;   // threads per CTA of the P2G/G2P kernels (particles per chunk / ppt)
+constexpr int kCtaThreads = 256;      // threads per CTA of the particle kernels
 constexpr int kMaxPpt = 4;            // particles per thread in one chunk, at most
 constexpr int kNodeChunk = 2048;      // grid nodes per work item of the grid kernel (small grids: fewer)
 constexpr int kSortTile = 4096;       // keys per CTA of a radix pass (256 threads x 16)

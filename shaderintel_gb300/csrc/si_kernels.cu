@@ -262,11 +262,11 @@ template <typename Fn>
 __device__ __forceinline__ void tile_walk(int ex, int ey, int ez, Fn&& f) {
   const int tid = threadIdx.x;
   const int exy = ex * ey;
-  const bool narrow = exy < kChunkThreads;
-  const int zs = narrow ? kChunkThreads / exy : 1;
+  const bool narrow = exy < kCtaThreads;
+  const int zs = narrow ? kCtaThreads / exy : 1;
   const int z0 = narrow ? tid / exy : 0;
   if (z0 >= zs) return;
-  for (int col = narrow ? tid - z0 * exy : tid; col < exy; col += narrow ? exy : kChunkThreads) {
+  for (int col = narrow ? tid - z0 * exy : tid; col < exy; col += narrow ? exy : kCtaThreads) {
     const int ly = col / ex, lx = col - ly * ex;
     for (int lz = z0; lz < ez; lz += zs) f(col + exy * lz, lx, ly, lz);
   }
@@ -318,7 +318,7 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
     atomicMin(&sbox[0], lo0); atomicMin(&sbox[1], lo1); atomicMin(&sbox[2], lo2);
     atomicMax(&sbox[3], hi0); atomicMax(&sbox[4], hi1); atomicMax(&sbox[5], hi2);
   }
-  if (sc == nullptr && tid == kChunkThreads / 2) { sbox[8] = reg.b[0]; sbox[9] = reg.b[1]; sbox[10] = reg.b[2]; }
+  if (sc == nullptr && tid == kCtaThreads / 2) { sbox[8] = reg.b[0]; sbox[9] = reg.b[1]; sbox[10] = reg.b[2]; }
   cta_sync();
   const int o0 = sbox[0], o1 = sbox[1], o2 = sbox[2];
   const int ex = sbox[3] - o0 + 3, ey = sbox[4] - o1 + 3, ez = sbox[5] - o2 + 3;
@@ -400,12 +400,12 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
 
 // ------------------------------------------------------------------ P2G kernel (mpm.js:306-401)
 template <int PPT>
-__global__ void __launch_bounds__(kChunkThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t) {
+__global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo t) {
   extern __shared__ __align__(16) int smem[];
   int* tile = smem;
   int* sbox = smem + 4 * kTileNodes;
   float* sc = reinterpret_cast<float*>(sbox + 24);
-  constexpr int chunk = kChunkThreads * PPT;
+  constexpr int chunk = kCtaThreads * PPT;
   box_empty(sbox);
   cta_sync();
   for (uint32_t c = blockIdx.x; c < t.pchunks; c += gridDim.x) {
@@ -421,14 +421,14 @@ __global__ void __launch_bounds__(kChunkThreads, SI_G2P_MIN_CTAS) k_p2g(TickInfo
     Scat reg;
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-      const bool valid = k * kChunkThreads + (int)threadIdx.x < count;
-      const int64_t i = first + min(k * kChunkThreads + (int)threadIdx.x, count - 1);
+      const bool valid = k * kCtaThreads + (int)threadIdx.x < count;
+      const int64_t i = first + min(k * kCtaThreads + (int)threadIdx.x, count - 1);
       float4 x = __ldg(&src[i]), v = __ldg(&src[cap + i]);
       float4 c0 = __ldg(&src[2 * cap + i]), c1 = __ldg(&src[3 * cap + i]), c2 = __ldg(&src[4 * cap + i]);
       float t01 = __ldg(&src[5 * cap + i].w), t02 = __ldg(&src[6 * cap + i].w), t12 = __ldg(&src[7 * cap + i].w);
       prep_scatter(reg, x, v, c0, c1, c2, t01, t02, t12, prm);
       if (!valid) scat_silence(reg);
-      if (PPT > 1) scat_store(sc, chunk, k * kChunkThreads + threadIdx.x, reg);
+      if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + threadIdx.x, reg);
     }
     cta_scatter(reg, true, PPT > 1 ? sc : nullptr, chunk, PPT > 1 ? chunk : count, dims,
                 reinterpret_cast<int*>(ts.grid), (flags & F_FORCE_GLOBAL) != 0, t.tile_nodes, tile, sbox, nullptr,
@@ -830,14 +830,14 @@ __device__ __forceinline__ void cta_base_box(const float4 (&xs)[PPT], int count,
 // pregathered scratch); ticks without one run the variant without that path.
 // FAST: the world decomposes snow and sand to a tolerance (si_world_set_svd_tolerance).
 template <int PPT, bool PRE, bool FAST>
-__global__ void __launch_bounds__(kChunkThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t, const uint32_t* __restrict__ perm) {
+__global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t, const uint32_t* __restrict__ perm) {
   extern __shared__ __align__(16) int smem[];
   int* tile = smem;
   float4* tilef = reinterpret_cast<float4*>(smem);
   int* gbox = smem + 4 * kTileNodes;   // box of the old stencils (gather tile)
   int* sbox = gbox + 8;                // box of the new bases (scatter tile) and its middle base
   float* sc = reinterpret_cast<float*>(gbox + 24);
-  constexpr int chunk = kChunkThreads * PPT;
+  constexpr int chunk = kCtaThreads * PPT;
   const int tid = threadIdx.x;
   // Chunks are handed out in order as CTAs become free: the first wave by CTA index, the rest from a
   // counter that thread 0 bumps at the start of a chunk for the CTA's next one (chunk costs differ by
@@ -875,7 +875,7 @@ __global__ void __launch_bounds__(kChunkThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo
     int64_t js[PPT];
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-      const int slot = min(k * kChunkThreads + tid, count - 1);
+      const int slot = min(k * kCtaThreads + tid, count - 1);
       js[k] = gather ? (int64_t)__ldg(&perm[ts.seg_base + first + slot]) : (int64_t)(first + slot);
       xs[k] = __ldcs(&Pin[js[k]]);
     }
@@ -899,8 +899,8 @@ __global__ void __launch_bounds__(kChunkThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo
     Scat reg;
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-      const bool valid = k * kChunkThreads + tid < count;
-      const int slot = min(k * kChunkThreads + tid, count - 1);
+      const bool valid = k * kCtaThreads + tid < count;
+      const int slot = min(k * kCtaThreads + tid, count - 1);
       const int64_t i = first + slot, j = js[k];
       // G2P reads x, J (v.w) and F; v.xyz, C and the stress are recomputed (mpm.js:479-559), so their
       // 52 bytes per particle are not loaded. A fluid's F is reset to I (mpm.js:520-525) and its input
@@ -925,7 +925,7 @@ __global__ void __launch_bounds__(kChunkThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo
       if (fuse) {
         prep_scatter(reg, x, v, c0, c1, c2, f0.w, f1.w, f2.w, prm);
         if (!valid) scat_silence(reg);
-        if (PPT > 1) scat_store(sc, chunk, k * kChunkThreads + tid, reg);
+        if (PPT > 1) scat_store(sc, chunk, k * kCtaThreads + tid, reg);
       }
     }
     // 4. P2G of the next substep through the same shared memory; it empties both boxes for the next
@@ -1019,7 +1019,7 @@ __global__ void k_instances(const float4* __restrict__ P, int64_t cap, int64_t o
 // ------------------------------------------------------------------ launchers
 int p2g_smem_bytes(int tile_nodes, int ppt) {
   (void)tile_nodes;
-  return kTileNodes * 16 + 96 + (ppt > 1 ? kScatWords * 4 * kChunkThreads * ppt : 0);
+  return kTileNodes * 16 + 96 + (ppt > 1 ? kScatWords * 4 * kCtaThreads * ppt : 0);
 }
 int max_tile_nodes() { return kTileNodes; }
 
@@ -1041,29 +1041,29 @@ static cudaError_t set_smem_attr(int tile_nodes) {
 void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st) {
   if (t.pchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
-  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kChunkThreads);
-  switch (t.chunk / kChunkThreads) {
-    case 1: k_p2g<1><<<ctas, kChunkThreads, smem, st>>>(t); break;
-    case 4: k_p2g<4><<<ctas, kChunkThreads, smem, st>>>(t); break;
-    default: k_p2g<2><<<ctas, kChunkThreads, smem, st>>>(t); break;
+  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kCtaThreads);
+  switch (t.chunk / kCtaThreads) {
+    case 1: k_p2g<1><<<ctas, kCtaThreads, smem, st>>>(t); break;
+    case 4: k_p2g<4><<<ctas, kCtaThreads, smem, st>>>(t); break;
+    default: k_p2g<2><<<ctas, kCtaThreads, smem, st>>>(t); break;
   }
 }
 template <int PPT>
 static void launch_g2p_ppt(const TickInfo& t, const uint32_t* perm, int ctas, int smem, cudaStream_t st, bool pre,
                            bool fast) {
   if (pre) {
-    if (fast) k_g2p<PPT, true, true><<<ctas, kChunkThreads, smem, st>>>(t, perm);
-    else k_g2p<PPT, true, false><<<ctas, kChunkThreads, smem, st>>>(t, perm);
+    if (fast) k_g2p<PPT, true, true><<<ctas, kCtaThreads, smem, st>>>(t, perm);
+    else k_g2p<PPT, true, false><<<ctas, kCtaThreads, smem, st>>>(t, perm);
   } else {
-    if (fast) k_g2p<PPT, false, true><<<ctas, kChunkThreads, smem, st>>>(t, perm);
-    else k_g2p<PPT, false, false><<<ctas, kChunkThreads, smem, st>>>(t, perm);
+    if (fast) k_g2p<PPT, false, true><<<ctas, kCtaThreads, smem, st>>>(t, perm);
+    else k_g2p<PPT, false, false><<<ctas, kCtaThreads, smem, st>>>(t, perm);
   }
 }
 void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st, bool pre, bool fast) {
   if (t.pchunks == 0) return;
   int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
-  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kChunkThreads);
-  switch (t.chunk / kChunkThreads) {
+  int smem = p2g_smem_bytes(t.tile_nodes, t.chunk / kCtaThreads);
+  switch (t.chunk / kCtaThreads) {
     case 1: launch_g2p_ppt<1>(t, perm, ctas, smem, st, pre, fast); break;
     case 4: launch_g2p_ppt<4>(t, perm, ctas, smem, st, pre, fast); break;
     default: launch_g2p_ppt<2>(t, perm, ctas, smem, st, pre, fast); break;
@@ -1143,14 +1143,14 @@ int occupancy_ctas(int which, int tile_nodes, int ppt) {
   int smem = p2g_smem_bytes(tile_nodes, ppt);
   switch (which) {
     case 0:
-      if (ppt == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<1>, kChunkThreads, smem);
-      else if (ppt == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<4>, kChunkThreads, smem);
-      else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<2>, kChunkThreads, smem);
+      if (ppt == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<1>, kCtaThreads, smem);
+      else if (ppt == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<4>, kCtaThreads, smem);
+      else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_p2g<2>, kCtaThreads, smem);
       break;
-    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<2, false, false>, kChunkThreads, smem); break;
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<2, false, false>, kCtaThreads, smem); break;
     case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_grid, kCtaThreads, 0); break;
-    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<1, false, false>, kChunkThreads, smem); break;
-    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<4, false, false>, kChunkThreads, smem); break;
+    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<1, false, false>, kCtaThreads, smem); break;
+    case 4: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_g2p<4, false, false>, kCtaThreads, smem); break;
     default: break;
   }
   return n > 0 ? n : 1;

@@ -282,7 +282,7 @@ static void finish_tick(si_world* w, HostTick& k) {
     k.nck.push_back((uint32_t)((k.nodes[e] + node_chunk - 1) / node_chunk));
   }
   uint32_t pc = 0, nc = 0, cc = 0, seg = 0, bin = 0;
-  const uint32_t chunk = (uint32_t)(kChunkThreads * w->ppt);
+  const uint32_t chunk = (uint32_t)(kCtaThreads * w->ppt);
   for (size_t e = 0; e < k.ts.size(); e++) {
     TickScene& t = k.ts[e];
     t.pchunk_begin = pc;
@@ -416,7 +416,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   t.pchunks = k.pchunks;
   t.nchunks = k.nchunks;
   t.cchunks = k.cchunks;
-  t.chunk = kChunkThreads * w->ppt;
+  t.chunk = kCtaThreads * w->ppt;
   t.tile_nodes = w->tile_nodes;
   t.nz = -0.0f;
   t.grid_done = w->grid_done;
@@ -802,11 +802,10 @@ int si_world_profile(si_world* w, int32_t enable, double ms_out[4], int32_t rese
 
 int si_world_set_tuning(si_world* w, int32_t particles_per_cta, int32_t tile_nodes, int32_t flush) {
   GUARD_WORLD(w);
-  if (particles_per_cta % kChunkThreads)
-    return si_fail(SI_EINVAL, "particles per CTA must be a multiple of " + std::to_string(kChunkThreads));
+  if (particles_per_cta % kCtaThreads) return si_fail(SI_EINVAL, "particles per CTA must be a multiple of 256");
   if (flush != 0 && flush != 1) return si_fail(SI_EINVAL, "flush strategy must be 0 (shared tile) or 1 (global)");
   CK(cudaStreamSynchronize(w->st));
-  int r = world_configure(w, particles_per_cta / kChunkThreads, tile_nodes);
+  int r = world_configure(w, particles_per_cta / kCtaThreads, tile_nodes);
   if (!r) w->flush = flush;
   return r;
 }
