@@ -745,17 +745,17 @@ __device__ __forceinline__ void g2p_update(const Gathered& g, float4& X, float4&
         const float Jold = (sv.x * sv.y) * sv.z;
         const float Jnew = (s.x * s.y) * s.z;
         vw = clampf((vw * Jold) / Jnew, 0.6f, 20.0f);
-        F = mm(mdiag_right(U, s), mT(Vm));
-        const float h = si_expf(m1.y * (1.0f - vw));
+        F = mmx<FAST>(mdiag_right(U, s), mT(Vm));
+        const float h = expx<FAST>(m1.y * (1.0f - vw));
         const float mu = mu0 * h, la = la0 * h;
-        const m3 R = mm(U, mT(Vm));
+        const m3 R = mmx<FAST>(U, mT(Vm));
         const float J = Jnew;
         const float tm = 2.0f * mu;
         m3 FR;
         FR.c[0] = vscale(tm, vsub(F.c[0], R.c[0]));
         FR.c[1] = vscale(tm, vsub(F.c[1], R.c[1]));
         FR.c[2] = vscale(tm, vsub(F.c[2], R.c[2]));
-        const m3 P1 = mm(FR, mT(F));
+        const m3 P1 = mmx<FAST>(FR, mT(F));
         const float l = (la * J) * (J - 1.0f);
         t00 = P1.c[0].x + l * 1.0f;
         t11 = P1.c[1].y + l * 1.0f;
@@ -764,8 +764,8 @@ __device__ __forceinline__ void g2p_update(const Gathered& g, float4& X, float4&
         t02 = P1.c[2].x + l * 0.0f;
         t12 = P1.c[2].y + l * 0.0f;
       } else {
-        v3 e = V(si_logf(fmaxf(fabsf(sv.x), 1e-4f)), si_logf(fmaxf(fabsf(sv.y), 1e-4f)),
-                 si_logf(fmaxf(fabsf(sv.z), 1e-4f)));
+        v3 e = V(logx<FAST>(fmaxf(fabsf(sv.x), 1e-4f)), logx<FAST>(fmaxf(fabsf(sv.y), 1e-4f)),
+                 logx<FAST>(fmaxf(fabsf(sv.z), 1e-4f)));
         const float tr = (e.x + e.y) + e.z;
         const float tr3 = tr / 3.0f;
         const v3 dev = V(e.x - tr3, e.y - tr3, e.z - tr3);
@@ -777,13 +777,13 @@ __device__ __forceinline__ void g2p_update(const Gathered& g, float4& X, float4&
           if (dg > 0.0f && devn > 1e-12f)
             e = V(e.x - (dg * dev.x) / devn, e.y - (dg * dev.y) / devn, e.z - (dg * dev.z) / devn);
         }
-        const v3 s = V(si_expf(e.x), si_expf(e.y), si_expf(e.z));
-        F = mm(mdiag_right(U, s), mT(Vm));
+        const v3 s = V(expx<FAST>(e.x), expx<FAST>(e.y), expx<FAST>(e.z));
+        F = mmx<FAST>(mdiag_right(U, s), mT(Vm));
         const float te = (e.x + e.y) + e.z;
         const float tm = 2.0f * mu0;
         const float lt = la0 * te;
         const v3 dd = V(tm * e.x + lt, tm * e.y + lt, tm * e.z + lt);
-        const m3 T = mm(mdiag_right(U, dd), mT(U));
+        const m3 T = mmx<FAST>(mdiag_right(U, dd), mT(U));
         t00 = T.c[0].x; t11 = T.c[1].y; t22 = T.c[2].z;
         t01 = T.c[1].x; t02 = T.c[2].x; t12 = T.c[2].y;
       }

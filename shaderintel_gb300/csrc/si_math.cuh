@@ -283,6 +283,16 @@ __device__ __forceinline__ v3 mv_fma(const m3& m, v3 v) {
            __fmaf_rn(m.c[2].z, v.z, __fmaf_rn(m.c[1].z, v.y, m.c[0].z * v.x)));
 }
 
+__device__ __forceinline__ m3 mm_fma(const m3& a, const m3& b) {
+  m3 r; r.c[0] = mv_fma(a, b.c[0]); r.c[1] = mv_fma(a, b.c[1]); r.c[2] = mv_fma(a, b.c[2]); return r;
+}
+// The products and transcendental functions of the snow and sand updates: the bit-exact forms, or
+// (FAST) fused products and the hardware approximations of log and exp (absolute error below 2^-21
+// for log on [0.5, 2], 2 ulp plus a term in |x| for exp).
+template <bool FAST> __device__ __forceinline__ m3 mmx(const m3& a, const m3& b) { return FAST ? mm_fma(a, b) : mm(a, b); }
+template <bool FAST> __device__ __forceinline__ float logx(float x) { return FAST ? __logf(x) : si_logf(x); }
+template <bool FAST> __device__ __forceinline__ float expx(float x) { return FAST ? __expf(x) : si_expf(x); }
+
 __device__ __forceinline__ void svd3_fast(const m3& F, m3& U, v3& s_out, m3& Vm) {
   m3 A;
 #pragma unroll
