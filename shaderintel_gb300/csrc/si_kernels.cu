@@ -272,7 +272,7 @@ __device__ __forceinline__ void tile_walk(int ex, int ey, int ez, Fn&& f) {
   }
 }
 
-// Layout of the scatter tile: when the padded box fits the tile, rows of tx nodes padded by two and
+// Layout of the scatter tile: when the padded box fits the tile, rows of tx nodes padded by one and
 // layers padded to a stride of 12 mod 32 words, so that lanes scattering into neighbouring rows and
 // layers meet fewer shared-memory bank conflicts (a CPU model of the sorted mixed scene: 3.9 -> 3.4
 // wavefronts per atomic); otherwise the dense layout, so that padding never makes a chunk overflow the
@@ -280,12 +280,18 @@ __device__ __forceinline__ void tile_walk(int ex, int ey, int ez, Fn&& f) {
 #ifndef SI_TILE_PAD
 #define SI_TILE_PAD 1
 #endif
+#ifndef SI_TILE_PADX
+#define SI_TILE_PADX 1    // nodes added to a row
+#endif
+#ifndef SI_TILE_LMOD
+#define SI_TILE_LMOD 12   // layer stride mod 32
+#endif
 __device__ __forceinline__ int tile_layer_stride_padded(int sy, int ty) {
   const int a = sy * ty;
-  return a + ((12 - (a & 31)) & 31);
+  return a + ((SI_TILE_LMOD - (a & 31)) & 31);
 }
 __device__ __forceinline__ long long tile_padded_nodes(int tx, int ty, int tz) {
-  return (long long)tile_layer_stride_padded(tx + 2, ty) * tz;
+  return (long long)tile_layer_stride_padded(tx + SI_TILE_PADX, ty) * tz;
 }
 
 // Side of the largest cube of nodes the tile holds (dense layout; tile_nodes >= 343).
@@ -374,7 +380,7 @@ __device__ __forceinline__ void cta_scatter(const Scat& reg, bool has_reg, const
       pad = false;
     }
   }
-  const int sy = pad ? tx + 2 : tx, sz = pad ? tile_layer_stride_padded(sy, ty) : sy * ty;
+  const int sy = pad ? tx + SI_TILE_PADX : tx, sz = pad ? tile_layer_stride_padded(sy, ty) : sy * ty;
   const int tnodes = use_tile ? sz * tz : 0;   // extent of the layout, padding included
   if (use_tile) {
     for (int t = tid; t < tnodes; t += blockDim.x) {
