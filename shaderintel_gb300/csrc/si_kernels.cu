@@ -770,18 +770,25 @@ __device__ __forceinline__ void g2p_update(const Gathered& g, float4& X, float4&
         const v3 s = V(clampf(sv.x, lo_s, hi_s), clampf(sv.y, lo_s, hi_s), clampf(sv.z, lo_s, hi_s));
         const float Jold = (sv.x * sv.y) * sv.z;
         const float Jnew = (s.x * s.y) * s.z;
-        vw = clampf((vw * Jold) / Jnew, 0.6f, 20.0f);
+        vw = clampf(divx<FAST>(vw * Jold, Jnew), 0.6f, 20.0f);
         F = mmx<FAST>(mdiag_right(U, s), mT(Vm));
         const float h = expx<FAST>(m1.y * (1.0f - vw));
         const float mu = mu0 * h, la = la0 * h;
-        const m3 R = mmx<FAST>(U, mT(Vm));
         const float J = Jnew;
         const float tm = 2.0f * mu;
-        m3 FR;
-        FR.c[0] = vscale(tm, vsub(F.c[0], R.c[0]));
-        FR.c[1] = vscale(tm, vsub(F.c[1], R.c[1]));
-        FR.c[2] = vscale(tm, vsub(F.c[2], R.c[2]));
-        const m3 P1 = mmx<FAST>(FR, mT(F));
+        m3 P1;
+        if (FAST) {
+          // 2 mu (F - R) F^T with F = U S V^T and R = U V^T is U diag(2 mu (s - 1) s) U^T
+          const v3 dd = V(tm * ((s.x - 1.0f) * s.x), tm * ((s.y - 1.0f) * s.y), tm * ((s.z - 1.0f) * s.z));
+          P1 = mm_fma(mdiag_right(U, dd), mT(U));
+        } else {
+          const m3 R = mm(U, mT(Vm));
+          m3 FR;
+          FR.c[0] = vscale(tm, vsub(F.c[0], R.c[0]));
+          FR.c[1] = vscale(tm, vsub(F.c[1], R.c[1]));
+          FR.c[2] = vscale(tm, vsub(F.c[2], R.c[2]));
+          P1 = mm(FR, mT(F));
+        }
         const float l = (la * J) * (J - 1.0f);
         t00 = P1.c[0].x + l * 1.0f;
         t11 = P1.c[1].y + l * 1.0f;
@@ -795,13 +802,19 @@ __device__ __forceinline__ void g2p_update(const Gathered& g, float4& X, float4&
         const float tr = (e.x + e.y) + e.z;
         const float tr3 = tr / 3.0f;
         const v3 dev = V(e.x - tr3, e.y - tr3, e.z - tr3);
-        const float devn = vlen(dev);
+        const float devn = sqrtx<FAST>(vdot(dev, dev));
         if (tr >= 0.0f) {
           e = V(0.0f, 0.0f, 0.0f);
         } else {
           const float dg = devn + (((3.0f * la0 + 2.0f * mu0) / (2.0f * mu0)) * tr) * m2.x;
-          if (dg > 0.0f && devn > 1e-12f)
-            e = V(e.x - (dg * dev.x) / devn, e.y - (dg * dev.y) / devn, e.z - (dg * dev.z) / devn);
+          if (dg > 0.0f && devn > 1e-12f) {
+            if (FAST) {
+              const float r = __fdividef(dg, devn);
+              e = V(__fmaf_rn(-r, dev.x, e.x), __fmaf_rn(-r, dev.y, e.y), __fmaf_rn(-r, dev.z, e.z));
+            } else {
+              e = V(e.x - (dg * dev.x) / devn, e.y - (dg * dev.y) / devn, e.z - (dg * dev.z) / devn);
+            }
+          }
         }
         const v3 s = V(expx<FAST>(e.x), expx<FAST>(e.y), expx<FAST>(e.z));
         F = mmx<FAST>(mdiag_right(U, s), mT(Vm));

@@ -296,6 +296,9 @@ __device__ __forceinline__ m3 mm_fma(const m3& a, const m3& b) {
 template <bool FAST> __device__ __forceinline__ m3 mmx(const m3& a, const m3& b) { return FAST ? mm_fma(a, b) : mm(a, b); }
 template <bool FAST> __device__ __forceinline__ float logx(float x) { return FAST ? __logf(x) : si_logf(x); }
 template <bool FAST> __device__ __forceinline__ float expx(float x) { return FAST ? __expf(x) : si_expf(x); }
+// Division and square root: IEEE, or (FAST) the fast division and x rsqrt(x) (x >= 0).
+template <bool FAST> __device__ __forceinline__ float divx(float a, float b) { return FAST ? __fdividef(a, b) : a / b; }
+template <bool FAST> __device__ __forceinline__ float sqrtx(float x) { return FAST ? (x > 0.0f ? x * rsqrtf(x) : 0.0f) : sqrtf(x); }
 
 __device__ __forceinline__ void svd3_fast(const m3& F, m3& U, v3& s_out, m3& Vm) {
   Sym3 A;
