@@ -918,6 +918,18 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
       js[k] = gather ? (int64_t)__ldg(&perm[ts.seg_base + first + slot]) : (int64_t)(first + slot);
       xs[k] = __ldcs(&Pin[js[k]]);
     }
+    // The loads of J (v.w) and, for the other models, F come after the staging barrier; start them
+    // into L1 now, while the box and the gather tile are built (prefetches hold no registers).
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+      const int64_t j = js[k];
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(reinterpret_cast<const float*>(&Pin[cin + j]) + 3));
+      if (__float_as_uint(__ldg(&prm->mats[(__float_as_uint(xs[k].w) & 7u) * 3].x)) != 0u) {
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(&Pin[fin + j]));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(&Pin[fin + cin + j]));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(&Pin[fin + 2 * cin + j]));
+      }
+    }
     cta_base_box<PPT>(xs, count, dims, gbox);
     const int o0 = gbox[0], o1 = gbox[1], o2 = gbox[2];
     const int ex = gbox[3] - o0 + 3, ey = gbox[4] - o1 + 3, ez = gbox[5] - o2 + 3;
