@@ -137,7 +137,7 @@ int si_mpm_read_instances(si_mpm* h, float* out, int64_t offset, int64_t n, uint
 /* Read-only device views for zero-copy interop (the reference hands layers its GPU buffers, MPM.P /
  * MPM.grid): what = 0..7 particle stream k (float4 per particle: x, v, c0, c1, c2, f0, f1, f2 of the
  * record), 8 the grid of the last grid update (int4 / vec4f per node), 9 the block keys of the last
- * sort (u32, pre-sort order, as si_mpm_read_bins), 10 the starts (u32, numBlocks + 1). *count = elements, *stride = bytes per element. Valid until the next
+ * sort (u32, pre-sort order, as si_mpm_read_bins; SI_EINVAL for a scene admitted to a server), 10 the starts (u32, numBlocks + 1). *count = elements, *stride = bytes per element. Valid until the next
  * call that steps, sorts, adds or destroys; the caller orders its reads after si_mpm_sync. */
 int si_mpm_device_ptr(si_mpm* h, int32_t what, const void** ptr, int64_t* count, int64_t* stride);
 int si_mpm_read_positions(si_mpm* h, float* xyz, int64_t offset, int64_t n);
@@ -173,7 +173,8 @@ int si_mpm_g2p(si_mpm* h);
 int si_mpm_read_grid(si_mpm* h, int32_t* nodes4);
 /* key and blockCount of the last sort, mpm.js:122-124: keys in the pre-sort particle order,
  * starts = the exclusive scan of the block counts (num_blocks + 1 entries, last = count).
- * Either pointer may be NULL. */
+ * Either pointer may be NULL. A scene admitted to a server keeps no keys: keys must be NULL for it
+ * (SI_EINVAL otherwise). */
 int si_mpm_read_bins(si_mpm* h, uint32_t* keys, uint32_t* starts);
 int si_mpm_sync(si_mpm* h);
 
@@ -284,14 +285,16 @@ typedef struct si_server_stats {
 /* The server steps `world` from its own thread until si_server_destroy; scenes already in the
  * world become resident. Edits of resident scenes stay allowed from any thread. Scenes created in
  * the world while it has a server keep one particle buffer instead of two (their sort substeps read
- * a gathered copy of the old state from the world's scratch); that scratch, and the sort's, are held
+ * a gathered copy of the old state from the world's scratch) and no block keys (their sorts key the
+ * positions as they start, so si_mpm_read_bins and si_mpm_device_ptr give their starts but refuse
+ * their keys with SI_EINVAL); the gathered copy and the sort's scratch are held
  * below min(2 GiB, budget / 32) by running a tick's scenes in groups, and that reserve counts
  * against the budget (si_server_stats.resident_bytes includes it). */
 int si_server_create(si_world* world, int64_t budget_bytes, si_server** out);
 int si_server_destroy(si_server* s);
 /* Admission by footprint: creates a resident scene if it fits the HBM budget, else SI_ENOMEM. The
- * footprint is 128 B x maxParticles (one particle buffer) + 32 B x grid nodes + 8 B x maxParticles
- * (block keys) + 4 B x (numBlocks + 1) + about 1.4 KB. */
+ * footprint is 128 B x maxParticles (one particle buffer) + 32 B x grid nodes + 4 B x (numBlocks + 1)
+ * + about 1.4 KB. */
 int si_server_admit(si_server* s, const si_mpm_desc* desc, si_mpm** out);
 /* Retires a scene (frees its HBM); pending requests on it complete with SI_EDESTROYED. */
 int si_server_retire(si_server* s, si_mpm* h);

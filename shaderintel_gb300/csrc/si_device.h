@@ -34,11 +34,13 @@ constexpr uint32_t F_FORCE_GLOBAL = 16u; // P2G skips the shared-memory tile (mp
 constexpr uint32_t F_NO_CLEAR_NEXT = 32u; // grid update leaves grid_next alone
 constexpr uint32_t F_KEYS_NOW = 64u;  // compute the block keys of the current positions before the sort
 constexpr uint32_t F_CLEAR = 128u;    // zero `grid` before the standalone P2G
-constexpr uint32_t F_BOXED = 256u;
+constexpr uint32_t F_BOXED = 256u;    // grid update: nodes outside box_cur + box_next are zero in both arrays
+constexpr uint32_t F_COUPLE = 512u;   // run the fluid <-> rigid coupling pass after the grid update
 constexpr uint32_t F_PREGATHER = 1024u; // with F_GATHER, a scene with one particle buffer: the read streams were
                                         // gathered into the world's scratch in sorted order (k_pregather),
                                         // and the G2P reads them there and writes P in place
-constexpr uint32_t F_COUPLE = 512u;   // run the fluid <-> rigid coupling pass after the grid update    // grid update: nodes outside box_cur + box_next are zero in both arrays
+constexpr uint32_t F_KEYS_FROM_X = 2048u; // with F_GATHER, a scene without key buffers: the sort's first kernel
+                                          // computes the block keys from the current positions
 
 struct SceneParams {             // per scene, device resident, rewritten when a value changes
   float4 mats[24];               // 8 materials x 3 vec4 (mpm.js:116)

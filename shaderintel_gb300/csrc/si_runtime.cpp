@@ -62,10 +62,10 @@ static uint32_t num_blocks_for(const int32_t d[3]) {
 }
 
 // Device bytes of a scene: particle buffers (two, or one for a compact scene), two grids, two key
-// buffers, the starts, the parameters and the boxes.
+// buffers (none for a compact scene), the starts, the parameters and the boxes.
 static int64_t scene_footprint(int64_t cap, int64_t nodes, uint32_t nb, bool compact) {
-  return (compact ? 1 : 2) * (int64_t)kStreams * 16 * cap + 2 * 16 * nodes + 2 * 4 * cap + 4 * ((int64_t)nb + 1) +
-         (int64_t)sizeof(SceneParams) + 64;
+  return (compact ? 1 : 2) * (int64_t)kStreams * 16 * cap + 2 * 16 * nodes + (compact ? 0 : 2 * 4 * cap) +
+         4 * ((int64_t)nb + 1) + (int64_t)sizeof(SceneParams) + 64;
 }
 
 int64_t scene_footprint_of(const si_mpm_desc* in, bool compact) {
@@ -332,8 +332,12 @@ static TickScene substep_entry(si_mpm* h) {
   uint32_t f = F_FUSE;
   if (h->w->flush) f |= F_FORCE_GLOBAL;
   if (!h->pending) { f |= F_P2G; if (!h->next_clear) f |= F_CLEAR; }
-  if (sort_now) { f |= F_GATHER; if (!h->keys_valid) f |= F_KEYS_NOW; if (h->compact) f |= F_PREGATHER; }
-  if (next_sort) f |= F_KEYS;
+  if (sort_now) {
+    f |= F_GATHER;
+    if (h->compact) f |= F_PREGATHER | F_KEYS_FROM_X;   // no key buffers: the sort keys the positions itself
+    else if (!h->keys_valid) f |= F_KEYS_NOW;
+  }
+  if (next_sort && !h->compact) f |= F_KEYS;
   if (sort_now) t.keys_next = h->keys[1 - h->kpend];   // the sort consumes keys[kpend]
   // both boxes are exact once two standard substeps ran in a row: box_cur from the P2G that filled
   // `grid` (the previous G2P, or the standalone P2G of a substep that started after box_ok was
@@ -389,7 +393,8 @@ static const TickScene* single_sort_scene(const HostTick& k) {
   int sorting = 0;
   for (const TickScene& e : k.ts)
     if (e.flags & F_GATHER) { sorting++; only = &e; }
-  return (sorting == 1 && only->seg_base == 0 && only->bin_base == 0) ? only : nullptr;
+  return (sorting == 1 && only->seg_base == 0 && only->bin_base == 0 && !(only->flags & F_KEYS_FROM_X)) ? only
+                                                                                                   : nullptr;
 }
 
 static int64_t tick_kernels(const HostTick& k) {
@@ -645,7 +650,7 @@ static int run_phase(si_mpm* h, int mode, uint32_t extra_flags) {
     case T_P2G: t.flags = F_P2G | F_CLEAR | extra_flags; break;
     case T_GRID: t.flags = F_NO_CLEAR_NEXT; break;
     case T_G2P: t.flags = 0; break;
-    case T_SORT: t.flags = F_GATHER | (h->keys_valid ? 0u : F_KEYS_NOW); break;
+    case T_SORT: t.flags = F_GATHER | (h->compact ? F_KEYS_FROM_X : (h->keys_valid ? 0u : F_KEYS_NOW)); break;
   }
   float4* fresh = nullptr;   // a compact scene's explicit sort reorders into a new buffer, then frees the old
   if (mode == T_SORT && h->compact) {
@@ -895,7 +900,7 @@ int scene_create(si_world* w, const si_mpm_desc* in, si_mpm** out, bool own_worl
   for (int b = 0; b < (h->compact ? 1 : 2) && e == cudaSuccess; b++)
     e = cudaMallocAsync((void**)&h->pbuf[b], std::max<size_t>(pbytes, 16), st);
   for (int b = 0; b < 2 && e == cudaSuccess; b++) e = cudaMallocAsync((void**)&h->grid[b], (size_t)h->nodes * 16, st);
-  for (int b = 0; b < 2 && e == cudaSuccess; b++)
+  for (int b = 0; b < (h->compact ? 0 : 2) && e == cudaSuccess; b++)   // a compact scene keeps no keys
     e = cudaMallocAsync((void**)&h->keys[b], std::max<size_t>(4 * (size_t)h->cap, 16), st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->starts, 4 * ((size_t)h->num_blocks + 1), st);
   if (e == cudaSuccess) e = cudaMallocAsync((void**)&h->prm, sizeof(SceneParams), st);
@@ -1243,6 +1248,7 @@ int si_mpm_device_ptr(si_mpm* h, int32_t what, const void** ptr, int64_t* count,
     *count = h->nodes;
     *stride = 16;
   } else if (what == 9) {
+    if (h->compact) return si_fail(SI_EINVAL, "si_mpm_device_ptr: a scene admitted to a server keeps no keys");
     *ptr = h->keys[1 - h->kpend];
     *count = h->count;
     *stride = 4;
@@ -1389,6 +1395,7 @@ int si_mpm_read_grid(si_mpm* h, int32_t* nodes4) {
 
 int si_mpm_read_bins(si_mpm* h, uint32_t* keys, uint32_t* starts) {
   GUARD(h);
+  if (keys && h->compact) return si_fail(SI_EINVAL, "si_mpm_read_bins: a scene admitted to a server keeps no keys");
   if (keys && h->count)
     CK(cudaMemcpyAsync(keys, h->keys[1 - h->kpend], (size_t)h->count * 4, cudaMemcpyDeviceToHost, h->w->st));
   if (starts)

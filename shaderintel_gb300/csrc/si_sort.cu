@@ -31,15 +31,25 @@ __device__ __forceinline__ int find_scene_p2(const TickScene* ts, int n, uint32_
   return lo;
 }
 
-// concatenated (key, local index) of the sorting scenes
+// concatenated (key, local index) of the sorting scenes; a scene without key buffers (F_KEYS_FROM_X)
+// has its block keys computed here from its current positions, as k_keys would
 __global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t* keys, uint32_t* vals) {
   for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
     const TickScene& ts = t.ts[find_scene_p2(t.ts, t.nscenes, chunk)];
     if (!(ts.flags & F_GATHER)) continue;
     const int first = (int)(chunk - ts.pchunk_begin) * t.chunk;
     const int last = min(first + t.chunk, ts.n);
+    const bool from_x = (ts.flags & F_KEYS_FROM_X) != 0;
+    const uint32_t nb = ts.prm->num_blocks;
     for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
-      keys[ts.seg_base + i] = ts.bin_base + ts.keys[i];
+      uint32_t k;
+      if (from_x) {
+        const float4 x = ts.P[i];
+        k = block_key(x.x, x.y, x.z, nb);
+      } else {
+        k = ts.keys[i];
+      }
+      keys[ts.seg_base + i] = ts.bin_base + k;
       vals[ts.seg_base + i] = (uint32_t)i;
     }
   }

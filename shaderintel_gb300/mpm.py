@@ -486,13 +486,14 @@ class MPM:
         check(L.lib().si_mpm_read_grid(self._h, out.ctypes.data_as(L.c_int32_p)))
         return out
 
-    def readBins(self):
-        n = self.count
-        keys = np.empty(n, np.uint32)
+    def readBins(self, keys=True):
+        """(keys, starts) of the last sort (mpm.js:122-124). A scene admitted to a server keeps no
+        keys: read it with keys=False, which returns (None, starts)."""
+        k = np.empty(self.count, np.uint32) if keys else None
         starts = np.empty(self.numBlocks + 1, np.uint32)
-        check(L.lib().si_mpm_read_bins(self._h, keys.ctypes.data_as(L.c_uint32_p),
+        check(L.lib().si_mpm_read_bins(self._h, k.ctypes.data_as(L.c_uint32_p) if keys else None,
                                        starts.ctypes.data_as(L.c_uint32_p)))
-        return keys, starts
+        return k, starts
 
     def sync(self):
         check(L.lib().si_mpm_sync(self._h))
