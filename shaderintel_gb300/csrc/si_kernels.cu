@@ -546,9 +546,28 @@ __global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
     const v3 hi = V((float)prm->dims[0] - bound, (float)prm->dims[1] - bound, (float)prm->dims[2] - bound);
     const int ncol = prm->ncol;
     const bool clear_next = !(ts.flags & F_NO_CLEAR_NEXT);
+    // the thread's node (lx, ly, lz) of the region is split once per chunk and then advanced by the
+    // CTA's stride without further divisions by the region's extents
+    const uint32_t nxr = (uint32_t)reg.nx, nyr = (uint32_t)reg.ny;
+    const uint32_t qy = blockDim.x / nxr, rx = blockDim.x - qy * nxr;
+    uint32_t lz, ly, lx;
+    {
+      const uint32_t r0 = (uint32_t)(first + threadIdx.x);
+      lz = r0 / rxy;
+      const uint32_t rem = r0 - lz * rxy;
+      ly = rem / nxr;
+      lx = rem - ly * nxr;
+    }
     for (int64_t r = first + threadIdx.x; r < last; r += blockDim.x) {
-      const uint32_t lz = (uint32_t)r / rxy, rem = (uint32_t)r - lz * rxy;
-      const uint32_t ly = rem / (uint32_t)reg.nx, lx = rem - ly * (uint32_t)reg.nx;
+      if (r != first + threadIdx.x) {
+        lx += rx;
+        ly += qy;
+        if (lx >= nxr) { lx -= nxr; ly++; }
+        if (ly >= nyr) {
+          if (ly < 2 * nyr) { ly -= nyr; lz++; }
+          else { lz += ly / nyr; ly -= (ly / nyr) * nyr; }
+        }
+      }
       const int64_t nxi = reg.x0 + lx, nyi = reg.y0 + ly, nzi = reg.z0 + lz;
       const int64_t i = nxi + X * (nyi + Y * nzi);
       int4 g = ts.grid[i];
