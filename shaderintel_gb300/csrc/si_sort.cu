@@ -39,18 +39,18 @@ __global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t*
     if (!(ts.flags & F_GATHER)) continue;
     const int first = (int)(chunk - ts.pchunk_begin) * t.chunk;
     const int last = min(first + t.chunk, ts.n);
-    const bool from_x = (ts.flags & F_KEYS_FROM_X) != 0;
-    const uint32_t nb = ts.prm->num_blocks;
-    for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
-      uint32_t k;
-      if (from_x) {
+    if (ts.flags & F_KEYS_FROM_X) {
+      const uint32_t nb = ts.prm->num_blocks;
+      for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
         const float4 x = ts.P[i];
-        k = block_key(x.x, x.y, x.z, nb);
-      } else {
-        k = ts.keys[i];
+        keys[ts.seg_base + i] = ts.bin_base + block_key(x.x, x.y, x.z, nb);
+        vals[ts.seg_base + i] = (uint32_t)i;
       }
-      keys[ts.seg_base + i] = ts.bin_base + k;
-      vals[ts.seg_base + i] = (uint32_t)i;
+    } else {
+      for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
+        keys[ts.seg_base + i] = ts.bin_base + ts.keys[i];
+        vals[ts.seg_base + i] = (uint32_t)i;
+      }
     }
   }
 }
