@@ -13,6 +13,8 @@
 #include "si_cuda.h"
 #include "si_device.h"
 #include "si_math.cuh"
+#include "si_region.cuh"
+
 
 namespace si {
 
@@ -22,20 +24,14 @@ namespace si {
 // arriving thread, so every thread of the CTA has passed the preceding phase when it completes.
 __device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: "memory"); }
 
-__device__ __forceinline__ int find_scene_p2(const TickScene* ts, int n, uint32_t chunk) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (ts[mid].pchunk_begin <= chunk) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 // concatenated (key, local index) of the sorting scenes; a scene without key buffers (F_KEYS_FROM_X)
 // has its block keys computed here from its current positions, as k_keys would
 __global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t* keys, uint32_t* vals) {
+  __shared__ uint32_t scene_tab[kSceneTable];
+  scene_table_load<false>(t, scene_tab);
+  __syncthreads();
   for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
-    const TickScene& ts = t.ts[find_scene_p2(t.ts, t.nscenes, chunk)];
+    const TickScene& ts = t.ts[scene_of<false>(t, scene_tab, chunk)];
     if (!(ts.flags & F_GATHER)) continue;
     const int first = (int)(chunk - ts.pchunk_begin) * t.chunk;
     const int last = min(first + t.chunk, ts.n);
