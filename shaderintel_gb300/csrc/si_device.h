@@ -117,6 +117,13 @@ struct SortInfo {                // one tick's sort
   const uint32_t* keys_in;       // one sorting scene at offset 0: its keys, read by the first pass
                                  // with identity indices (no concatenation), else nullptr
   uint32_t* starts_out;          // that scene's starts (written by the one-CTA sort), else nullptr
+  // Segmented sort (keys_in == nullptr): every sorting scene's keys are its own block keys, its
+  // segment starts on a tile boundary and is padded to whole tiles with `sentinel` (above every key),
+  // and each pass ranks digits within a scene's tiles only, so the passes cover the largest scene's
+  // key range instead of the tick's total bins.
+  uint32_t* tile_scene;          // tiles: the tick-table index of the scene a tile belongs to
+  uint32_t* seg_total;           // scenes x 256: a scene's digit totals of the current pass
+  uint32_t sentinel;
 };
 
 // One sorting scene small enough for the one-CTA sort (k_small_sort): its keys and per-warp bin

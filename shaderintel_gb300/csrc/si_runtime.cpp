@@ -251,6 +251,7 @@ struct HostTick {
   bool any_p2g = false, any_clear = false, any_gather = false, any_keys_now = false, any_pregather = false;
   uint32_t sort_n = 0, sort_bins = 0, max_blocks = 0;
   int passes = 0;
+  uint32_t sentinel = 0;   // segmented sort: the key that pads each scene's segment to whole tiles
 };
 
 static TickScene base_entry(si_mpm* h) {
@@ -283,6 +284,15 @@ static void finish_tick(si_world* w, HostTick& k) {
   }
   uint32_t pc = 0, nc = 0, cc = 0, seg = 0, bin = 0;
   const uint32_t chunk = (uint32_t)(kCtaThreads * w->ppt);
+  // One sorting scene with its own keys is sorted in place of the concatenation (its keys feed the
+  // first pass directly); otherwise the sort is segmented: each sorting scene keeps its own block keys,
+  // its segment starts on a tile boundary and is padded to whole tiles, and the passes cover the
+  // largest scene's keys rather than the tick's total bins.
+  int sorting = 0;
+  bool any_from_x = false;
+  for (const TickScene& t : k.ts)
+    if (t.flags & F_GATHER) { sorting++; if (t.flags & F_KEYS_FROM_X) any_from_x = true; }
+  const bool segmented = sorting > 1 || any_from_x;
   for (size_t e = 0; e < k.ts.size(); e++) {
     TickScene& t = k.ts[e];
     t.pchunk_begin = pc;
@@ -297,8 +307,8 @@ static void finish_tick(si_world* w, HostTick& k) {
     if (t.flags & F_GATHER) {
       k.any_gather = true;
       t.seg_base = seg;
-      t.bin_base = bin;
-      seg += (uint32_t)t.n;
+      t.bin_base = segmented ? 0u : bin;
+      seg += segmented ? (((uint32_t)t.n + kSortTile - 1) / kSortTile) * kSortTile : (uint32_t)t.n;
       bin += k.nb[e];
       k.max_blocks = std::max(k.max_blocks, k.nb[e]);
     }
@@ -309,9 +319,12 @@ static void finish_tick(si_world* w, HostTick& k) {
   k.cchunks = cc;
   k.sort_n = seg;
   k.sort_bins = bin;
+  // key range: the tick's bins, or (segmented) the largest scene's bins plus the sentinel above them
+  const uint64_t range = segmented ? (uint64_t)k.max_blocks + 1 : std::max<uint32_t>(bin, 2u);
   int bits = 1;
-  while (bits < 32 && (1ull << bits) < (uint64_t)std::max<uint32_t>(bin, 2u)) bits++;
+  while (bits < 32 && (1ull << bits) < range) bits++;
   k.passes = (bits + kRadixBits - 1) / kRadixBits;
+  k.sentinel = segmented ? (k.passes * kRadixBits >= 32 ? 0xffffffffu : (1u << (k.passes * kRadixBits)) - 1u) : 0u;
 }
 
 static void push_entry(HostTick& k, const si_mpm* h, const TickScene& t) {
@@ -360,7 +373,7 @@ static TickScene substep_entry(si_mpm* h) {
   return t;
 }
 
-static int ensure_sort_scratch(si_world* w, uint32_t n) {
+static int ensure_sort_scratch(si_world* w, uint32_t n, uint32_t scenes) {
   const size_t need = (size_t)std::max<uint32_t>(n, 1u) * 4;
   if (need > w->sort_cap) {
     size_t cap = std::max(need, w->sort_cap + w->sort_cap / 2);
@@ -383,6 +396,22 @@ static int ensure_sort_scratch(si_world* w, uint32_t n) {
     world_free_graphs(w);
   }
   if (!w->digit_total) CK(cudaMallocAsync((void**)&w->digit_total, 256 * 4, w->st));
+  // segmented sort: the scene of every tile, and every scene's digit totals of the current pass
+  const size_t need_ts = tiles * 4, need_st = (size_t)std::max<uint32_t>(scenes, 1u) * 256 * 4;
+  if (need_ts > w->tile_scene_cap) {
+    void* q = w->tile_scene;
+    int r = ensure_dev(w, &q, &w->tile_scene_cap, need_ts);
+    if (r) return r;
+    w->tile_scene = (uint32_t*)q;
+    world_free_graphs(w);
+  }
+  if (need_st > w->seg_total_cap) {
+    void* q = w->seg_total;
+    int r = ensure_dev(w, &q, &w->seg_total_cap, need_st);
+    if (r) return r;
+    w->seg_total = (uint32_t*)q;
+    world_free_graphs(w);
+  }
   return SI_OK;
 }
 
@@ -439,6 +468,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
     s.n = k.sort_n; s.bins = k.sort_bins; s.passes = k.passes;
     s.keys_a = w->ka; s.vals_a = w->va; s.keys_b = w->kb; s.vals_b = w->vb;
     s.hist = w->hist; s.digit_total = w->digit_total;
+    s.tile_scene = w->tile_scene; s.seg_total = w->seg_total; s.sentinel = k.sentinel;
     const TickScene* only = single_sort_scene(k);
     s.keys_in = only ? only->keys : nullptr;
     s.starts_out = only ? only->starts : nullptr;
@@ -489,12 +519,13 @@ static bool same_plan(const GraphPlan& g, const std::vector<HostTick>& plan, con
 
 static int run_plan(si_world* w, std::vector<HostTick>& plan) {
   if (plan.empty()) return SI_OK;
-  uint32_t max_sort = 0, max_pre = 0;
+  uint32_t max_sort = 0, max_pre = 0, max_scenes = 0;
   for (const HostTick& k : plan) {
     max_sort = std::max(max_sort, k.sort_n);
+    max_scenes = std::max(max_scenes, (uint32_t)k.ts.size());
     if (k.any_pregather) max_pre = std::max(max_pre, k.sort_n);
   }
-  int r = ensure_sort_scratch(w, max_sort);
+  int r = ensure_sort_scratch(w, max_sort, max_scenes);
   if (r) return r;
   if (max_pre > w->gscratch_cap) {   // the pregather scratch, grown like the sort's (graphs hold its address)
     if (w->gscratch) CK(cudaFreeAsync(w->gscratch, w->st));
@@ -616,14 +647,15 @@ int run_substeps(si_world* w, const std::vector<si_mpm*>& scenes, int K) {
     int64_t sorting = 0;
     for (si_mpm* h : act) {
       const bool sorts = h->sort_every > 0 && h->step_count % h->sort_every == 0;
-      if (sorts && w->group_particles > 0 && sorting > 0 && sorting + h->count > w->group_particles) {
+      const int64_t slots = (h->count + kSortTile - 1) / kSortTile * kSortTile;   // its padded segment
+      if (sorts && w->group_particles > 0 && sorting > 0 && sorting + slots > w->group_particles) {
         finish_tick(w, k);
         plan.push_back(std::move(k));
         k = HostTick();
         k.mode = T_SUBSTEP;
         sorting = 0;
       }
-      if (sorts) sorting += h->count;
+      if (sorts) sorting += slots;
       push_entry(k, h, substep_entry(h));
     }
     finish_tick(w, k);
@@ -744,7 +776,7 @@ int si_world_destroy(si_world* w) {
   for (si_mpm* h : sc) scene_release(h);
   world_free_graphs(w);
   for (void* p : {(void*)w->ka, (void*)w->va, (void*)w->kb, (void*)w->vb, (void*)w->hist, (void*)w->digit_total,
-                  (void*)w->tab, (void*)w->grid_done, (void*)w->gscratch})
+                  (void*)w->tile_scene, (void*)w->seg_total, (void*)w->tab, (void*)w->grid_done, (void*)w->gscratch})
     if (p) cudaFreeAsync(p, w->st);
   cudaStreamSynchronize(w->st);
   for (auto& e : w->pev) if (e) cudaEventDestroy(e);

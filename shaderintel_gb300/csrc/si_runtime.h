@@ -51,6 +51,10 @@ struct si_world {
   uint32_t* hist = nullptr;
   size_t hist_cap = 0;
   uint32_t* digit_total = nullptr;
+  uint32_t* tile_scene = nullptr;   // segmented sort: scene of every tile
+  size_t tile_scene_cap = 0;
+  uint32_t* seg_total = nullptr;    // segmented sort: 256 digit totals per scene of a tick
+  size_t seg_total_cap = 0;
   // One-buffer scenes (created while `compact` is set, as a server's are): their sort substeps
   // gather the G2P's inputs into this scratch (kPregatherStreams x 16 B per sorting particle), and a
   // tick whose sorting particles exceed group_particles runs as several groups of scenes, so the

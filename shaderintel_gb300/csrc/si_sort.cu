@@ -24,17 +24,32 @@ namespace si {
 // arriving thread, so every thread of the CTA has passed the preceding phase when it completes.
 __device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: "memory"); }
 
-// concatenated (key, local index) of the sorting scenes; a scene without key buffers (F_KEYS_FROM_X)
-// has its block keys computed here from its current positions, as k_keys would
-__global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t* keys, uint32_t* vals) {
+// Concatenated (key, local index) of the sorting scenes, each scene's segment starting on a tile
+// boundary (seg_base) and padded to whole tiles with the sentinel key; tile_scene[tile] names the
+// scene of every tile. A scene without key buffers (F_KEYS_FROM_X) has its block keys computed here
+// from its current positions, as k_keys would.
+__global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t* keys, uint32_t* vals,
+                                                           uint32_t* tile_scene, uint32_t sentinel) {
   __shared__ uint32_t scene_tab[kSceneTable];
   scene_table_load<false>(t, scene_tab);
   __syncthreads();
   for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
-    const TickScene& ts = t.ts[scene_of<false>(t, scene_tab, chunk)];
+    const int scene = scene_of<false>(t, scene_tab, chunk);
+    const TickScene& ts = t.ts[scene];
     if (!(ts.flags & F_GATHER)) continue;
     const int first = (int)(chunk - ts.pchunk_begin) * t.chunk;
     const int last = min(first + t.chunk, ts.n);
+    // tiles whose first slot lies in this chunk (every tile of a segment starts inside the scene:
+    // the padding is shorter than a tile)
+    for (int i = first + threadIdx.x; i < last; i += blockDim.x)
+      if ((i & (kSortTile - 1)) == 0) tile_scene[(ts.seg_base + (uint32_t)i) / kSortTile] = (uint32_t)scene;
+    if (last == ts.n) {   // the scene's last chunk pads its segment to whole tiles
+      const int end = (ts.n + kSortTile - 1) & ~(kSortTile - 1);
+      for (int i = ts.n + threadIdx.x; i < end; i += blockDim.x) {
+        keys[ts.seg_base + i] = sentinel;
+        vals[ts.seg_base + i] = (uint32_t)i;
+      }
+    }
     if (ts.flags & F_KEYS_FROM_X) {
       const uint32_t nb = ts.prm->num_blocks;
       for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
@@ -107,17 +122,65 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
   if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
 }
 
+// The segmented form of k_radix_scan: per digit, the exclusive prefix over the tiles of each scene
+// (restarting where tile_scene changes), and each scene's digit total into seg_total[scene][digit].
+__global__ void __launch_bounds__(kCtaThreads) k_radix_scan_seg(uint32_t* hist, uint32_t tiles,
+                                                               const uint32_t* __restrict__ tile_scene,
+                                                               uint32_t* seg_total) {
+  __shared__ uint32_t warp_sum[kWarps];
+  __shared__ uint32_t warp_head[kWarps];
+  __shared__ uint32_t carry;
+  const uint32_t d = blockIdx.x;
+  uint32_t* row = hist + (size_t)d * tiles;
+  if (threadIdx.x == 0) carry = 0;
+  cta_sync();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t b = 0; b < tiles; b += kCtaThreads) {
+    const uint32_t i = b + threadIdx.x;
+    const bool in = i < tiles;
+    const uint32_t v = in ? row[i] : 0u;
+    const uint32_t sc = in ? __ldg(&tile_scene[i]) : 0xffffffffu;
+    const bool head = in && (i == 0 || __ldg(&tile_scene[i - 1]) != sc);
+    const bool tail = in && (i + 1 == tiles || __ldg(&tile_scene[i + 1]) != sc);
+    // inclusive segmented scan of (v, head) within the warp
+    uint32_t x = v, f = head ? 1u : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      const uint32_t g = __shfl_up_sync(0xffffffffu, f, o);
+      if (lane >= o && !f) { x += y; f = g; }
+    }
+    if (lane == 31) { warp_sum[warp] = x; warp_head[warp] = f; }
+    cta_sync();
+    // the earlier warps' part of this element's segment, then the carry of the earlier tiles
+    if (!f) {
+      for (int w = warp - 1; w >= 0 && !f; w--) { x += warp_sum[w]; f = warp_head[w]; }
+      if (!f) x += carry;
+    }
+    if (in) {
+      row[i] = x - v;
+      if (tail) seg_total[(size_t)sc * 256 + d] = x;
+    }
+    cta_sync();   // every thread has read carry and the warp sums
+    if (i == min(b + kCtaThreads, tiles) - 1) carry = x;   // the block's last tile: its segment goes on
+    cta_sync();
+  }
+}
+
 // Stable scatter of one pass. Warp w of a tile owns the kSortTile / kWarps consecutive keys from
 // tile * kSortTile + w * kSeg; it counts their digits (one add per distinct digit and round, by the
 // group's lowest lane), a per-digit prefix over the warps turns the counts into each warp's first
 // position, and a second walk over the same keys stores each at that position plus its rank among
 // the earlier lanes of its round with the same digit. The rank order is (warp, round, lane), which is
 // the keys' order in the tile, so equal digits keep their input order. vin == nullptr stands for the
-// identity (the value of key e is e).
+// identity (the value of key e is e). SEG: the segmented sort, where a tile's digit bases are its
+// scene's segment start plus the exclusive scan of that scene's digit totals.
+template <bool SEG>
 __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                               uint32_t* kout, uint32_t* vout, uint32_t n, int shift,
                                                               const uint32_t* __restrict__ hist, const uint32_t* __restrict__ digit_total,
-                                                              uint32_t tiles) {
+                                                              uint32_t tiles, const uint32_t* __restrict__ tile_scene,
+                                                              const uint32_t* __restrict__ seg_total, const TickScene* ts) {
   constexpr int kSeg = kSortTile / kWarps;   // 512 keys per warp, kItems rounds of 32
   static_assert(kSeg == kItems * 32, "a warp's segment is kItems rounds of 32 keys");
   __shared__ uint32_t dbase[256];
@@ -125,7 +188,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* _
   __shared__ uint32_t wsum[kWarps];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // exclusive scan of the digit totals (same in every CTA)
-  {
+  if (!SEG) {
     uint32_t v = digit_total[tid], x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -141,6 +204,19 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* _
   const unsigned lt_mask = (1u << lane) - 1u;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     for (int w = 0; w < kWarps; w++) woff[w][tid] = 0;
+    uint32_t sv = 0, sx = 0, sbase = 0;   // SEG: this digit's total in the tile's scene, its inclusive scan
+    if (SEG) {
+      const uint32_t scene = __ldg(&tile_scene[tile]);
+      sbase = ts[scene].seg_base;
+      sv = __ldg(&seg_total[(size_t)scene * 256 + tid]);
+      sx = sv;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, sx, o);
+        if (lane >= o) sx += y;
+      }
+      if (lane == 31) wsum[warp] = sx;
+    }
     cta_sync();
     const uint32_t wbase = tile * kSortTile + (uint32_t)warp * kSeg;
     uint32_t key[kItems], val[kItems];
@@ -159,7 +235,15 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scatter(const uint32_t* _
     cta_sync();
     // 2. per digit: the first position of each warp's keys (tile base of the digit from the scan)
     {
-      uint32_t acc = dbase[tid] + hist[tid * tiles + tile];
+      uint32_t db;
+      if (SEG) {
+        uint32_t pre = 0;
+        for (int w = 0; w < warp; w++) pre += wsum[w];
+        db = sbase + pre + sx - sv;
+      } else {
+        db = dbase[tid];
+      }
+      uint32_t acc = db + hist[tid * tiles + tile];
 #pragma unroll
       for (int w = 0; w < kWarps; w++) {
         const uint32_t c = woff[w][tid];
@@ -308,7 +392,7 @@ bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
   }
   if (!s.keys_in) {
     int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
-    k_sort_init<<<ctas, kCtaThreads, 0, st>>>(t, s.keys_a, s.vals_a);
+    k_sort_init<<<ctas, kCtaThreads, 0, st>>>(t, s.keys_a, s.vals_a, s.tile_scene, s.sentinel);
   }
   const uint32_t tiles = (s.n + kSortTile - 1) / kSortTile;
   uint32_t *ka = s.keys_a, *va = s.vals_a, *kb = s.keys_b, *vb = s.vals_b;
@@ -318,8 +402,15 @@ bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
     const uint32_t* kin = (p == 0 && s.keys_in) ? s.keys_in : ka;
     const uint32_t* vin = (p == 0 && s.keys_in) ? nullptr : va;
     k_radix_hist<<<ctas, kCtaThreads, 0, st>>>(kin, s.n, shift, s.hist, tiles);
-    k_radix_scan<<<256, kCtaThreads, 0, st>>>(s.hist, tiles, s.digit_total);
-    k_radix_scatter<<<ctas, kCtaThreads, 0, st>>>(kin, vin, kb, vb, s.n, shift, s.hist, s.digit_total, tiles);
+    if (s.keys_in) {
+      k_radix_scan<<<256, kCtaThreads, 0, st>>>(s.hist, tiles, s.digit_total);
+      k_radix_scatter<false><<<ctas, kCtaThreads, 0, st>>>(kin, vin, kb, vb, s.n, shift, s.hist, s.digit_total, tiles,
+                                                          nullptr, nullptr, nullptr);
+    } else {   // segmented: the concatenation of the sorting scenes, each sorted within its own tiles
+      k_radix_scan_seg<<<256, kCtaThreads, 0, st>>>(s.hist, tiles, s.tile_scene, s.seg_total);
+      k_radix_scatter<true><<<ctas, kCtaThreads, 0, st>>>(kin, vin, kb, vb, s.n, shift, s.hist, nullptr, tiles,
+                                                         s.tile_scene, s.seg_total, t.ts);
+    }
     uint32_t* tk = ka; ka = kb; kb = tk;
     uint32_t* tv = va; va = vb; vb = tv;
   }
@@ -432,7 +523,8 @@ extern "C" int si_block_sort_noalloc(const float* x, int64_t stride_floats, int3
     const int shift = p * kRadixBits;
     k_radix_hist<<<tiles, kCtaThreads, 0, st>>>(ka, (uint32_t)n, shift, hist, tiles);
     k_radix_scan<<<256, kCtaThreads, 0, st>>>(hist, tiles, digit_total);
-    k_radix_scatter<<<tiles, kCtaThreads, 0, st>>>(ka, va, kb, vb, (uint32_t)n, shift, hist, digit_total, tiles);
+    k_radix_scatter<false><<<tiles, kCtaThreads, 0, st>>>(ka, va, kb, vb, (uint32_t)n, shift, hist, digit_total, tiles,
+                                                         nullptr, nullptr, nullptr);
     std::swap(ka, kb);
     std::swap(va, vb);
   }
@@ -504,8 +596,8 @@ static int spatial_sort(si_spatial* g, const float4* pos, int64_t n) {
     for (int p = 0; p < passes; p++) {
       k_radix_hist<<<tiles, kCtaThreads, 0, st>>>(ka, (uint32_t)n, p * kRadixBits, g->hist, tiles);
       k_radix_scan<<<256, kCtaThreads, 0, st>>>(g->hist, tiles, g->digit_total);
-      k_radix_scatter<<<tiles, kCtaThreads, 0, st>>>(ka, va, kb, vb, (uint32_t)n, p * kRadixBits, g->hist,
-                                                     g->digit_total, tiles);
+      k_radix_scatter<false><<<tiles, kCtaThreads, 0, st>>>(ka, va, kb, vb, (uint32_t)n, p * kRadixBits, g->hist,
+                                                            g->digit_total, tiles, nullptr, nullptr, nullptr);
       std::swap(ka, kb);
       std::swap(va, vb);
     }
