@@ -1,12 +1,13 @@
 // si_sort.cu — the block sort of mpm.js:563-577/614-621 for one tick of many scenes.
 //
 // The reference counts keys with global atomics, so the order inside a block depends on atomic
-// timing. Here the particles of every sorting scene are concatenated with key = bin_base + block key
-// and sorted by a stable LSD radix sort (8-bit digits; per pass: tile histograms, a scan per digit,
-// a stable scatter in which each warp ranks a contiguous segment of its tile with warp match and
-// per-warp digit counters). It is deterministic, has no waits between CTAs, and yields the
-// reference's counts and starts exactly; each scene's particles stay inside its own segment because
-// the bin ranges are ordered like the segments.
+// timing. Here the particles are sorted by a stable LSD radix sort (8-bit digits; per pass: tile
+// histograms, a scan per digit, a stable scatter in which each warp ranks a contiguous segment of its
+// tile with warp match and per-warp digit counters). One sorting scene is sorted from its own keys;
+// the sorting scenes of a tick of several are concatenated into tile-aligned segments, each padded
+// with a sentinel key and sorted within its own tiles (a segmented scan of the tile histograms), so
+// the passes cover the largest scene's keys. It is deterministic, has no waits between CTAs, and
+// yields the reference's counts and starts exactly.
 #include <algorithm>
 #include <mutex>
 
