@@ -137,3 +137,31 @@ def test_scene_added_and_destroyed_mid_batch():
         assert np.array_equal(bits(scenes[k].readParticles()), bits(want[k]))
     ref.destroy()
     w.destroy()
+
+
+def test_segmented_sort_tile_edges():
+    """Scenes whose particle counts sit on either side of the sort's 4096-key tiles (1, 4095, 4096,
+    4097, 8193) sorted in one tick: each scene's segment is padded to whole tiles, so every count
+    exercises another padding; the records after two sorts equal the scenes stepped alone."""
+    src = make(None, (48, (10, 3, 12), (20, 16, 18), "sand", (1.0, 0.0, -0.5)))
+    src.step(dt=src.substepDt, K=2)
+    rec = src.readParticles()
+    src.destroy()
+    counts = [1, 4095, 4096, 4097, 8193]
+
+    def scene(world, n):
+        sim = MPM(world, grid=48, maxParticles=n, substeps=8)
+        sim._material("sand")
+        assert sim.addRecords(rec[:n]) == n
+        return sim
+
+    w = World()
+    batch_sims = [scene(w, n) for n in counts]
+    w.step(8)                                   # sorts at the first and fifth substep
+    for n, b in zip(counts, batch_sims):
+        a = scene(None, n)
+        a.step(dt=a.substepDt, K=8)
+        assert np.array_equal(bits(a.readParticles()), bits(b.readParticles())), n
+        assert all(np.array_equal(x, y) for x, y in zip(a.readBins(), b.readBins())), n
+        a.destroy()
+    w.destroy()
