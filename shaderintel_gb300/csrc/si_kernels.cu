@@ -532,10 +532,10 @@ __device__ __forceinline__ float collider_sdf(uint32_t kind, v3 d, float4 s) {
 
 __global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
   __shared__ uint32_t scene_tab[kSceneTable];
-  scene_table_load<true>(t, scene_tab);
+  scene_table_load<kSceneN>(t, scene_tab);
   __syncthreads();
   for (uint32_t chunk = blockIdx.x; chunk < t.nchunks; chunk += gridDim.x) {
-    const TickScene& ts = t.ts[scene_of<true>(t, scene_tab, chunk)];
+    const TickScene& ts = t.ts[scene_of<kSceneN>(t, scene_tab, chunk)];
     const SceneParams* prm = ts.prm;
     const int64_t X = prm->dims[0], Y = prm->dims[1];
     const NodeRegion reg = grid_region(ts, prm->dims);
@@ -906,14 +906,14 @@ __global__ void __launch_bounds__(kCtaThreads, SI_G2P_MIN_CTAS) k_g2p(TickInfo t
   // alternates so that a chunk's write cannot meet a slow warp's read of the previous one.
   __shared__ uint32_t next_chunk[2];
   __shared__ uint32_t scene_tab[kSceneTable];
-  scene_table_load<false>(t, scene_tab);
+  scene_table_load<kSceneP>(t, scene_tab);
   box_empty(gbox);
   box_empty(sbox);
   cta_sync();
   uint32_t parity = 0;
   for (uint32_t c = blockIdx.x; c < t.pchunks; c = next_chunk[parity], parity ^= 1u) {
     if (tid == 0) next_chunk[parity] = gridDim.x + atomicAdd(&t.g2p_sched[0], 1u);
-    const TickScene& ts = t.ts[scene_of<false>(t, scene_tab, c)];
+    const TickScene& ts = t.ts[scene_of<kSceneP>(t, scene_tab, c)];
     const uint32_t flags = ts.flags;
     const SceneParams* prm = ts.prm;
     const int first = (int)(c - ts.pchunk_begin) * chunk;

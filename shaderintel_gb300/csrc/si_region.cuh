@@ -25,24 +25,31 @@ __device__ __forceinline__ NodeRegion grid_region(const TickScene& ts, const int
   return r;
 }
 
-// The first chunk of each scene of a tick (pchunk_begin, or nchunk_begin for NODES), copied into
-// shared memory by each CTA once per launch when the tick has at most kSceneTable scenes: a chunk's
-// scene is then found by a binary search in shared memory instead of one through the tick table in
-// global memory (eight dependent loads for 256 scenes, on lines the particle streams evict from L1).
+// A per-scene prefix of the tick table (FIELD: kSceneP the first particle chunk, kSceneN the first
+// node chunk, kSceneSeg the first slot of the scene's sort segment), copied into shared memory by each
+// CTA once per launch when the tick has at most kSceneTable scenes: the scene of a chunk or slot is
+// then found by a binary search in shared memory instead of one through the tick table in global
+// memory (eight dependent loads for 256 scenes, on lines the particle streams evict from L1).
 constexpr int kSceneTable = 1024;
-template <bool NODES>
+enum { kSceneP = 0, kSceneN = 1, kSceneSeg = 2 };
+template <int FIELD>
+__device__ __forceinline__ uint32_t scene_field(const TickScene& e) {
+  return FIELD == kSceneP ? e.pchunk_begin : (FIELD == kSceneN ? e.nchunk_begin : e.seg_base);
+}
+template <int FIELD>
 __device__ __forceinline__ void scene_table_load(const TickInfo& t, uint32_t* tab) {
   if (t.nscenes <= kSceneTable)
-    for (int i = threadIdx.x; i < t.nscenes; i += blockDim.x) tab[i] = NODES ? t.ts[i].nchunk_begin : t.ts[i].pchunk_begin;
+    for (int i = threadIdx.x; i < t.nscenes; i += blockDim.x) tab[i] = scene_field<FIELD>(t.ts[i]);
 }
-template <bool NODES>
-__device__ __forceinline__ int scene_of(const TickInfo& t, const uint32_t* tab, uint32_t chunk) {
+// the last scene whose prefix is <= x
+template <int FIELD>
+__device__ __forceinline__ int scene_of(const TickInfo& t, const uint32_t* tab, uint32_t x) {
   const bool shared_tab = t.nscenes <= kSceneTable;
   int lo = 0, hi = t.nscenes - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    const uint32_t b = shared_tab ? tab[mid] : (NODES ? t.ts[mid].nchunk_begin : t.ts[mid].pchunk_begin);
-    if (b <= chunk) lo = mid; else hi = mid - 1;
+    const uint32_t b = shared_tab ? tab[mid] : scene_field<FIELD>(t.ts[mid]);
+    if (b <= x) lo = mid; else hi = mid - 1;
   }
   return lo;
 }

@@ -304,9 +304,9 @@ static void finish_tick(si_world* w, HostTick& k) {
     if (t.flags & F_CLEAR) k.any_clear = true;
     if (t.flags & F_KEYS_NOW) k.any_keys_now = true;
     if (t.flags & F_PREGATHER) k.any_pregather = true;
+    t.seg_base = seg;   // a scene that does not sort sits at the running end with no slots
     if (t.flags & F_GATHER) {
       k.any_gather = true;
-      t.seg_base = seg;
       t.bin_base = segmented ? 0u : bin;
       seg += segmented ? (((uint32_t)t.n + kSortTile - 1) / kSortTile) * kSortTile : (uint32_t)t.n;
       bin += k.nb[e];

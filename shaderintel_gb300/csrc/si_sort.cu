@@ -27,40 +27,36 @@ __device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: 
 
 // Concatenated (key, local index) of the sorting scenes, each scene's segment starting on a tile
 // boundary (seg_base) and padded to whole tiles with the sentinel key; tile_scene[tile] names the
-// scene of every tile. A scene without key buffers (F_KEYS_FROM_X) has its block keys computed here
-// from its current positions, as k_keys would.
+// scene of every tile. A CTA fills whole tiles: the tile's scene is the last scene whose seg_base is
+// at most the tile's first slot (scenes that do not sort sit at the running end with no slots), found
+// in shared memory, so the tick table is read once per 4096 slots. A scene without key buffers
+// (F_KEYS_FROM_X) has its block keys computed here from its current positions, as k_keys would.
 __global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t* keys, uint32_t* vals,
-                                                           uint32_t* tile_scene, uint32_t sentinel) {
+                                                           uint32_t* tile_scene, uint32_t sentinel, uint32_t tiles) {
   __shared__ uint32_t scene_tab[kSceneTable];
-  scene_table_load<false>(t, scene_tab);
+  scene_table_load<kSceneSeg>(t, scene_tab);
   __syncthreads();
-  for (uint32_t chunk = blockIdx.x; chunk < t.pchunks; chunk += gridDim.x) {
-    const int scene = scene_of<false>(t, scene_tab, chunk);
+  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t slot0 = tile * kSortTile;
+    const int scene = scene_of<kSceneSeg>(t, scene_tab, slot0);
     const TickScene& ts = t.ts[scene];
-    if (!(ts.flags & F_GATHER)) continue;
-    const int first = (int)(chunk - ts.pchunk_begin) * t.chunk;
-    const int last = min(first + t.chunk, ts.n);
-    // tiles whose first slot lies in this chunk (every tile of a segment starts inside the scene:
-    // the padding is shorter than a tile)
-    for (int i = first + threadIdx.x; i < last; i += blockDim.x)
-      if ((i & (kSortTile - 1)) == 0) tile_scene[(ts.seg_base + (uint32_t)i) / kSortTile] = (uint32_t)scene;
-    if (last == ts.n) {   // the scene's last chunk pads its segment to whole tiles
-      const int end = (ts.n + kSortTile - 1) & ~(kSortTile - 1);
-      for (int i = ts.n + threadIdx.x; i < end; i += blockDim.x) {
-        keys[ts.seg_base + i] = sentinel;
-        vals[ts.seg_base + i] = (uint32_t)i;
-      }
-    }
+    if (threadIdx.x == 0) tile_scene[tile] = (uint32_t)scene;
+    const int n = ts.n;
+    const int first = (int)(slot0 - ts.seg_base);
     if (ts.flags & F_KEYS_FROM_X) {
       const uint32_t nb = ts.prm->num_blocks;
-      for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
-        const float4 x = ts.P[i];
-        keys[ts.seg_base + i] = ts.bin_base + block_key(x.x, x.y, x.z, nb);
+      for (int i = first + threadIdx.x; i < first + kSortTile; i += blockDim.x) {
+        uint32_t k = sentinel;
+        if (i < n) {
+          const float4 x = ts.P[i];
+          k = block_key(x.x, x.y, x.z, nb);
+        }
+        keys[ts.seg_base + i] = k;
         vals[ts.seg_base + i] = (uint32_t)i;
       }
     } else {
-      for (int i = first + threadIdx.x; i < last; i += blockDim.x) {
-        keys[ts.seg_base + i] = ts.bin_base + ts.keys[i];
+      for (int i = first + threadIdx.x; i < first + kSortTile; i += blockDim.x) {
+        keys[ts.seg_base + i] = i < n ? __ldg(&ts.keys[i]) : sentinel;
         vals[ts.seg_base + i] = (uint32_t)i;
       }
     }
@@ -391,11 +387,11 @@ bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
     k_small_sort<<<1, kSmallThreads, smem, st>>>(s.keys_in, s.n, s.bins, s.keys_a, s.vals_a, s.starts_out);
     return true;
   }
-  if (!s.keys_in) {
-    int ctas = (int)std::min<uint32_t>(t.pchunks, (uint32_t)grid_ctas);
-    k_sort_init<<<ctas, kCtaThreads, 0, st>>>(t, s.keys_a, s.vals_a, s.tile_scene, s.sentinel);
-  }
   const uint32_t tiles = (s.n + kSortTile - 1) / kSortTile;
+  if (!s.keys_in) {
+    int ctas = (int)std::min<uint32_t>(tiles, (uint32_t)grid_ctas);
+    k_sort_init<<<ctas, kCtaThreads, 0, st>>>(t, s.keys_a, s.vals_a, s.tile_scene, s.sentinel, tiles);
+  }
   uint32_t *ka = s.keys_a, *va = s.vals_a, *kb = s.keys_b, *vb = s.vals_b;
   for (int p = 0; p < s.passes; p++) {
     const int shift = p * kRadixBits;
