@@ -138,7 +138,7 @@ inline bool small_sort_ok(uint32_t n, uint32_t bins, bool single) {
 // ---- launchers (si_kernels.cu / si_sort.cu); all enqueue on `st`.
 void launch_p2g(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_clear(const TickInfo& t, int grid_ctas, cudaStream_t st);
-void launch_grid(const TickInfo& t, int grid_ctas, cudaStream_t st);
+void launch_grid(const TickInfo& t, int grid_ctas, int grid_ctas_wide, cudaStream_t st);
 void launch_box_reset(const TickInfo& t, cudaStream_t st);
 void launch_couple(const TickInfo& t, int grid_ctas, cudaStream_t st);
 void launch_g2p(const TickInfo& t, const uint32_t* perm, int grid_ctas, cudaStream_t st,

@@ -132,6 +132,7 @@ int world_configure(si_world* w, int ppt, int tile_nodes) {
   w->ctas_p2g = w->sms * occupancy_ctas(0, tile_nodes, ppt);
   w->ctas_g2p = w->sms * occupancy_ctas(which_g2p, tile_nodes, ppt);
   w->ctas_grid = w->sms * occupancy_ctas(2, tile_nodes, ppt);
+  w->ctas_grid_wide = w->sms * occupancy_ctas(5, tile_nodes, ppt);
   w->ctas_misc = w->sms * 4;
   w->ctas_couple = w->sms * couple_ctas_per_sm();
   cudaGetLastError();
@@ -480,7 +481,7 @@ static void enqueue_tick(si_world* w, const HostTick& k, const TickScene* dev_ta
   if (k.any_clear) launch_clear(t, w->ctas_grid, st);
   if (k.any_p2g) launch_p2g(t, w->ctas_p2g, st);
   if (profile) cudaEventRecord(w->pev[2], st);
-  if (k.mode == T_SUBSTEP || k.mode == T_GRID) launch_grid(t, w->ctas_grid, st);
+  if (k.mode == T_SUBSTEP || k.mode == T_GRID) launch_grid(t, w->ctas_grid, w->ctas_grid_wide, st);
   if (k.cchunks) launch_couple(t, w->ctas_couple, st);
   if (k.mode == T_SUBSTEP && !t.reset_boxes) launch_box_reset(t, st);   // box_next starts empty for the fused P2G
   if (profile) cudaEventRecord(w->pev[3], st);

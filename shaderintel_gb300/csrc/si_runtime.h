@@ -44,7 +44,7 @@ struct si_world {
   // tuning (autotuner: particles per CTA = 256 * ppt, shared tile capacity in nodes)
   int ppt = 1, tile_nodes = 2048;
   int flush = 0;                    // P2G flush: 0 shared tile + non-zero node flush, 1 global atomics
-  int ctas_p2g = 0, ctas_g2p = 0, ctas_grid = 0, ctas_misc = 0, ctas_couple = 0;
+  int ctas_p2g = 0, ctas_g2p = 0, ctas_grid = 0, ctas_grid_wide = 0, ctas_misc = 0, ctas_couple = 0;
   // sort scratch (grown on demand)
   uint32_t *ka = nullptr, *va = nullptr, *kb = nullptr, *vb = nullptr;
   size_t sort_cap = 0;
