@@ -530,102 +530,110 @@ __device__ __forceinline__ float collider_sdf(uint32_t kind, v3 d, float4 s) {
   return vdot(d, V(s.x, s.y, s.z));
 }
 
-__device__ __forceinline__ void grid_update(const TickInfo& t) {
+// The nodes [first, last) of a scene's region (flat region order), thread tid from first + tid at
+// the CTA's stride.
+__device__ __forceinline__ void grid_nodes(const TickScene& ts, const NodeRegion& reg, int64_t first, int64_t last) {
+  const SceneParams* prm = ts.prm;
+  const int64_t X = prm->dims[0], Y = prm->dims[1];
+  const float bound = prm->bound, ff = prm->floor_friction;
+  const float g0 = prm->gravity[0], g1 = prm->gravity[1], g2 = prm->gravity[2];
+  const v3 hi = V((float)prm->dims[0] - bound, (float)prm->dims[1] - bound, (float)prm->dims[2] - bound);
+  const int ncol = prm->ncol;
+  const bool clear_next = !(ts.flags & F_NO_CLEAR_NEXT);
+  // the thread's node (lx, ly, lz) of the region is split once and then advanced by the CTA's
+  // stride without further divisions by the region's extents
+  const uint32_t nxr = (uint32_t)reg.nx, nyr = (uint32_t)reg.ny, rxy = nxr * nyr;
+  const uint32_t qy = blockDim.x / nxr, rx = blockDim.x - qy * nxr;
+  uint32_t lz, ly, lx;
+  {
+    const uint32_t r0 = (uint32_t)(first + threadIdx.x);
+    lz = r0 / rxy;
+    const uint32_t rem = r0 - lz * rxy;
+    ly = rem / nxr;
+    lx = rem - ly * nxr;
+  }
+  for (int64_t r = first + threadIdx.x; r < last; r += blockDim.x) {
+    if (r != first + threadIdx.x) {
+      lx += rx;
+      ly += qy;
+      if (lx >= nxr) { lx -= nxr; ly++; }
+      if (ly >= nyr) {
+        if (ly < 2 * nyr) { ly -= nyr; lz++; }
+        else { lz += ly / nyr; ly -= (ly / nyr) * nyr; }
+      }
+    }
+    const int64_t nxi = reg.x0 + lx, nyi = reg.y0 + ly, nzi = reg.z0 + lz;
+    const int64_t i = nxi + X * (nyi + Y * nzi);
+    int4 g = ts.grid[i];
+    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (g.w > 0) {
+      const float inv = 1.0f / 4194304.0f;
+      float m = (float)g.w * inv;
+      v3 v = V(((float)g.x * inv) / m + g0, ((float)g.y * inv) / m + g1, ((float)g.z * inv) / m + g2);
+      v3 c = V((float)nxi, (float)nyi, (float)nzi);
+      if (c.y < bound && v.y < 0.0f) {
+        float vn = -v.y;
+        v.y = 0.0f;
+        float vt = sqrtf(v.x * v.x + v.z * v.z);
+        if (vt > 1e-9f) {
+          float f = fmaxf(0.0f, 1.0f - (ff * vn) / vt);
+          v = V(v.x * f, 0.0f, v.z * f);
+        }
+      }
+      if (c.x < bound && v.x < 0.0f) v.x = 0.0f;
+      if (c.z < bound && v.z < 0.0f) v.z = 0.0f;
+      if (c.x > hi.x && v.x > 0.0f) v.x = 0.0f;
+      if (c.y > hi.y && v.y > 0.0f) v.y = 0.0f;
+      if (c.z > hi.z && v.z > 0.0f) v.z = 0.0f;
+      for (int k = 0; k < ncol; k++) {
+        const float4 h = prm->cols[3 * k], s = prm->cols[3 * k + 1], cvv = prm->cols[3 * k + 2];
+        const v3 cv = V(cvv.x, cvv.y, cvv.z);
+        const uint32_t kind = __float_as_uint(h.x);
+        const v3 d = V(c.x - h.y, c.y - h.z, c.z - h.w);
+        float dist = collider_sdf(kind, d, s);
+        if (dist < 1.0f) {
+          const float e = 0.5f;
+          v3 nr = V(collider_sdf(kind, V(d.x + e, d.y, d.z), s) - collider_sdf(kind, V(d.x - e, d.y, d.z), s),
+                    collider_sdf(kind, V(d.x, d.y + e, d.z), s) - collider_sdf(kind, V(d.x, d.y - e, d.z), s),
+                    collider_sdf(kind, V(d.x, d.y, d.z + e), s) - collider_sdf(kind, V(d.x, d.y, d.z - e), s));
+          nr = V(nr.x + 0.0f, nr.y + 1e-7f, nr.z + 0.0f);
+          float ln = vlen(nr);
+          nr = V(nr.x / ln, nr.y / ln, nr.z / ln);
+          v3 vr = vsub(v, cv);
+          float vn = vdot(vr, nr);
+          if (vn < 0.0f) {
+            vr = vsub(vr, vscale(vn, nr));
+            float vt = vlen(vr);
+            if (vt > 1e-9f) vr = vscale(fmaxf(0.0f, 1.0f - (s.w * -vn) / vt), vr);
+            v = vadd(vr, cv);
+          }
+        }
+      }
+      out = make_float4(v.x, v.y, v.z, m);
+    }
+    if ((g.x | g.y | g.z | g.w) != 0) reinterpret_cast<float4*>(ts.grid)[i] = out;   // zero stays zero
+    if (clear_next) ts.grid_next[i] = make_int4(0, 0, 0, 0);
+  }
+}
+
+// Every scene's region in node chunks of the host's table (ticks of several scenes).
+__device__ __forceinline__ void grid_chunks(const TickInfo& t) {
   __shared__ uint32_t scene_tab[kSceneTable];
   scene_table_load<kSceneN>(t, scene_tab);
   __syncthreads();
   for (uint32_t chunk = blockIdx.x; chunk < t.nchunks; chunk += gridDim.x) {
     const TickScene& ts = t.ts[scene_of<kSceneN>(t, scene_tab, chunk)];
-    const SceneParams* prm = ts.prm;
-    const int64_t X = prm->dims[0], Y = prm->dims[1];
-    const NodeRegion reg = grid_region(ts, prm->dims);
-    const uint32_t rxy = (uint32_t)reg.nx * (uint32_t)reg.ny;
-    const int64_t nodes = (int64_t)rxy * reg.nz;
+    const NodeRegion reg = grid_region(ts, ts.prm->dims);
+    const int64_t nodes = (int64_t)reg.nx * reg.ny * reg.nz;
     const int64_t first = (int64_t)(chunk - ts.nchunk_begin) * ts.node_chunk;
     if (first >= nodes) continue;
-    const int64_t last = min(first + (int64_t)ts.node_chunk, nodes);
-    const float bound = prm->bound, ff = prm->floor_friction;
-    const float g0 = prm->gravity[0], g1 = prm->gravity[1], g2 = prm->gravity[2];
-    const v3 hi = V((float)prm->dims[0] - bound, (float)prm->dims[1] - bound, (float)prm->dims[2] - bound);
-    const int ncol = prm->ncol;
-    const bool clear_next = !(ts.flags & F_NO_CLEAR_NEXT);
-    // the thread's node (lx, ly, lz) of the region is split once per chunk and then advanced by the
-    // CTA's stride without further divisions by the region's extents
-    const uint32_t nxr = (uint32_t)reg.nx, nyr = (uint32_t)reg.ny;
-    const uint32_t qy = blockDim.x / nxr, rx = blockDim.x - qy * nxr;
-    uint32_t lz, ly, lx;
-    {
-      const uint32_t r0 = (uint32_t)(first + threadIdx.x);
-      lz = r0 / rxy;
-      const uint32_t rem = r0 - lz * rxy;
-      ly = rem / nxr;
-      lx = rem - ly * nxr;
-    }
-    for (int64_t r = first + threadIdx.x; r < last; r += blockDim.x) {
-      if (r != first + threadIdx.x) {
-        lx += rx;
-        ly += qy;
-        if (lx >= nxr) { lx -= nxr; ly++; }
-        if (ly >= nyr) {
-          if (ly < 2 * nyr) { ly -= nyr; lz++; }
-          else { lz += ly / nyr; ly -= (ly / nyr) * nyr; }
-        }
-      }
-      const int64_t nxi = reg.x0 + lx, nyi = reg.y0 + ly, nzi = reg.z0 + lz;
-      const int64_t i = nxi + X * (nyi + Y * nzi);
-      int4 g = ts.grid[i];
-      float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (g.w > 0) {
-        const float inv = 1.0f / 4194304.0f;
-        float m = (float)g.w * inv;
-        v3 v = V(((float)g.x * inv) / m + g0, ((float)g.y * inv) / m + g1, ((float)g.z * inv) / m + g2);
-        v3 c = V((float)nxi, (float)nyi, (float)nzi);
-        if (c.y < bound && v.y < 0.0f) {
-          float vn = -v.y;
-          v.y = 0.0f;
-          float vt = sqrtf(v.x * v.x + v.z * v.z);
-          if (vt > 1e-9f) {
-            float f = fmaxf(0.0f, 1.0f - (ff * vn) / vt);
-            v = V(v.x * f, 0.0f, v.z * f);
-          }
-        }
-        if (c.x < bound && v.x < 0.0f) v.x = 0.0f;
-        if (c.z < bound && v.z < 0.0f) v.z = 0.0f;
-        if (c.x > hi.x && v.x > 0.0f) v.x = 0.0f;
-        if (c.y > hi.y && v.y > 0.0f) v.y = 0.0f;
-        if (c.z > hi.z && v.z > 0.0f) v.z = 0.0f;
-        for (int k = 0; k < ncol; k++) {
-          const float4 h = prm->cols[3 * k], s = prm->cols[3 * k + 1], cvv = prm->cols[3 * k + 2];
-          const v3 cv = V(cvv.x, cvv.y, cvv.z);
-          const uint32_t kind = __float_as_uint(h.x);
-          const v3 d = V(c.x - h.y, c.y - h.z, c.z - h.w);
-          float dist = collider_sdf(kind, d, s);
-          if (dist < 1.0f) {
-            const float e = 0.5f;
-            v3 nr = V(collider_sdf(kind, V(d.x + e, d.y, d.z), s) - collider_sdf(kind, V(d.x - e, d.y, d.z), s),
-                      collider_sdf(kind, V(d.x, d.y + e, d.z), s) - collider_sdf(kind, V(d.x, d.y - e, d.z), s),
-                      collider_sdf(kind, V(d.x, d.y, d.z + e), s) - collider_sdf(kind, V(d.x, d.y, d.z - e), s));
-            nr = V(nr.x + 0.0f, nr.y + 1e-7f, nr.z + 0.0f);
-            float ln = vlen(nr);
-            nr = V(nr.x / ln, nr.y / ln, nr.z / ln);
-            v3 vr = vsub(v, cv);
-            float vn = vdot(vr, nr);
-            if (vn < 0.0f) {
-              vr = vsub(vr, vscale(vn, nr));
-              float vt = vlen(vr);
-              if (vt > 1e-9f) vr = vscale(fmaxf(0.0f, 1.0f - (s.w * -vn) / vt), vr);
-              v = vadd(vr, cv);
-            }
-          }
-        }
-        out = make_float4(v.x, v.y, v.z, m);
-      }
-      if ((g.x | g.y | g.z | g.w) != 0) reinterpret_cast<float4*>(ts.grid)[i] = out;   // zero stays zero
-      if (clear_next) ts.grid_next[i] = make_int4(0, 0, 0, 0);
-    }
+    grid_nodes(ts, reg, first, min(first + (int64_t)ts.node_chunk, nodes));
   }
-  // The CTA that finishes last empties box_next of every scene for the fused P2G of the G2P that
-  // follows: every CTA has read the boxes (grid_region) before it counted itself done.
+}
+
+// The CTA that finishes last empties box_next of every scene for the fused P2G of the G2P that
+// follows: every CTA has read the boxes (grid_region) before it counted itself done.
+__device__ __forceinline__ void grid_boxes_reset(const TickInfo& t) {
   if (t.reset_boxes) {
     __shared__ bool last;
     __syncthreads();
@@ -647,11 +655,31 @@ __device__ __forceinline__ void grid_update(const TickInfo& t) {
   }
 }
 
-// The grid update at the register budget of three CTAs per SM (single scenes: measured best), and
-// at four CTAs per SM (64 registers) for ticks of several scenes, whose many small boxed regions gain
-// from the extra warps (batched substep -0.7 %, single scenes +5 % in the grid phase).
-__global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) { grid_update(t); }
-__global__ void __launch_bounds__(kCtaThreads, 4) k_grid_wide(TickInfo t) { grid_update(t); }
+// The grid update of a tick of one scene (three CTAs per SM).
+__global__ void __launch_bounds__(kCtaThreads) k_grid(TickInfo t) {
+  if (t.nscenes == 1) {
+    // One scene: its boxed region split evenly over the launch's CTAs, one piece each (multiples of
+    // 32 nodes). The host's node chunks cover the whole grid, so taking the region's first chunks
+    // left whatever exceeded one wave of CTAs to a second wave of a few (grid phase of the mixed
+    // scene -9 %, plasticity -16 %).
+    const TickScene& ts = t.ts[0];
+    const NodeRegion reg = grid_region(ts, ts.prm->dims);
+    const int64_t nodes = (int64_t)reg.nx * reg.ny * reg.nz;
+    const int64_t per = ((nodes + gridDim.x - 1) / gridDim.x + 31) & ~(int64_t)31;
+    const int64_t first = (int64_t)blockIdx.x * per;
+    if (first < nodes) grid_nodes(ts, reg, first, min(first + per, nodes));
+  } else {
+    grid_chunks(t);
+  }
+  grid_boxes_reset(t);
+}
+// The grid update of a tick of several scenes, at four CTAs per SM (64 registers): their many small
+// boxed regions gain from the extra warps (batched substep -0.7 %, single scenes +5 % in the grid
+// phase).
+__global__ void __launch_bounds__(kCtaThreads, 4) k_grid_wide(TickInfo t) {
+  grid_chunks(t);
+  grid_boxes_reset(t);
+}
 
 // Empties box_next of every scene of the tick: the fused P2G of the G2P that follows rebuilds it.
 __global__ void k_box_reset(TickInfo t) {
