@@ -272,19 +272,35 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_radix_scatter(const uint32_t
   }
 }
 
-// starts of every bin of every sorting scene: lower_bound in the sorted keys of its segment
-__global__ void k_scene_starts(TickInfo t, const uint32_t* __restrict__ skeys) {
+// starts of every bin of every sorting scene: lower_bound in the sorted keys of its segment. Every
+// stride-th key (stride = ceil(n / kStartSamples)) is first loaded into shared memory by the whole CTA
+// with independent loads; a bin's search narrows to one run of stride keys there and continues in
+// global memory only inside that run (11 dependent global loads instead of 21 for 2.2 M keys).
+constexpr uint32_t kStartSamples = 1024;
+__global__ void __launch_bounds__(256) k_scene_starts(TickInfo t, const uint32_t* __restrict__ skeys) {
+  __shared__ uint32_t smp[kStartSamples];
   const TickScene& ts = t.ts[blockIdx.y];
   if (!(ts.flags & F_GATHER)) return;
-  uint32_t* starts = ts.starts;
   const uint32_t nb = ts.prm->num_blocks;
+  if (blockIdx.x * blockDim.x > nb) return;          // no bin of this scene for the CTA
+  uint32_t* starts = ts.starts;
   const uint32_t* seg = skeys + ts.seg_base;
   const uint32_t n = (uint32_t)ts.n;
+  const uint32_t stride = (n + kStartSamples - 1) / kStartSamples;   // 0 only when n == 0
+  const uint32_t m = stride ? (n + stride - 1) / stride : 0;        // samples: seg[j * stride], j < m
+  for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) smp[j] = __ldg(&seg[j * stride]);
+  __syncthreads();
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= nb; k += gridDim.x * blockDim.x) {
     const uint32_t target = ts.bin_base + k;
-    uint32_t lo = 0, hi = n;
+    uint32_t a = 0, b = m;                           // the first sample >= target (m: none)
+    while (a < b) {
+      const uint32_t mid = (a + b) >> 1;
+      if (smp[mid] < target) a = mid + 1; else b = mid;
+    }
+    // seg[(a - 1) * stride] < target <= seg[a * stride]: the bound is in [(a - 1) * stride + 1, a * stride]
+    uint32_t lo = a ? (a - 1) * stride + 1 : 0, hi = min(a * stride, n);
     while (lo < hi) {
-      uint32_t mid = (lo + hi) >> 1;
+      const uint32_t mid = (lo + hi) >> 1;
       if (__ldg(&seg[mid]) < target) lo = mid + 1; else hi = mid;
     }
     starts[k] = lo;
