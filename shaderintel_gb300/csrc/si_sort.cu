@@ -25,46 +25,60 @@ namespace si {
 // arriving thread, so every thread of the CTA has passed the preceding phase when it completes.
 __device__ __forceinline__ void cta_sync() { asm volatile("barrier.sync 0;" ::: "memory"); }
 
+constexpr int kItems = kSortTile / kCtaThreads;   // 16
+constexpr int kWarps = kCtaThreads / 32;          // 8
+
 // Concatenated (key, local index) of the sorting scenes, each scene's segment starting on a tile
 // boundary (seg_base) and padded to whole tiles with the sentinel key; tile_scene[tile] names the
 // scene of every tile. A CTA fills whole tiles: the tile's scene is the last scene whose seg_base is
 // at most the tile's first slot (scenes that do not sort sit at the running end with no slots), found
 // in shared memory, so the tick table is read once per 4096 slots. A scene without key buffers
-// (F_KEYS_FROM_X) has its block keys computed here from its current positions, as k_keys would.
+// (F_KEYS_FROM_X) has its block keys computed here from its current positions, as k_keys would. The
+// tile histogram of the first pass (digit 0, as k_radix_hist counts it) is taken on the way, so that
+// pass does not read the keys back.
 __global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t* keys, uint32_t* vals,
-                                                           uint32_t* tile_scene, uint32_t sentinel, uint32_t tiles) {
+                                                           uint32_t* tile_scene, uint32_t sentinel, uint32_t tiles,
+                                                           uint32_t* hist) {
   __shared__ uint32_t scene_tab[kSceneTable];
+  __shared__ uint32_t h[256];
   scene_table_load<kSceneSeg>(t, scene_tab);
-  __syncthreads();
+  const unsigned lane = threadIdx.x & 31u;
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    h[threadIdx.x] = 0;
+    cta_sync();
     const uint32_t slot0 = tile * kSortTile;
     const int scene = scene_of<kSceneSeg>(t, scene_tab, slot0);
     const TickScene& ts = t.ts[scene];
     if (threadIdx.x == 0) tile_scene[tile] = (uint32_t)scene;
     const int n = ts.n;
     const int first = (int)(slot0 - ts.seg_base);
-    if (ts.flags & F_KEYS_FROM_X) {
-      const uint32_t nb = ts.prm->num_blocks;
-      for (int i = first + threadIdx.x; i < first + kSortTile; i += blockDim.x) {
-        uint32_t k = sentinel;
-        if (i < n) {
+    const bool from_x = (ts.flags & F_KEYS_FROM_X) != 0;
+    const uint32_t nb = from_x ? ts.prm->num_blocks : 0u;
+#pragma unroll 4
+    for (int r = 0; r < kItems; r++) {
+      const int i = first + r * kCtaThreads + (int)threadIdx.x;
+      uint32_t k = sentinel;
+      if (i < n) {
+        if (from_x) {
           const float4 x = ts.P[i];
           k = block_key(x.x, x.y, x.z, nb);
+        } else {
+          k = __ldg(&ts.keys[i]);
         }
-        keys[ts.seg_base + i] = k;
-        vals[ts.seg_base + i] = (uint32_t)i;
       }
-    } else {
-      for (int i = first + threadIdx.x; i < first + kSortTile; i += blockDim.x) {
-        keys[ts.seg_base + i] = i < n ? __ldg(&ts.keys[i]) : sentinel;
-        vals[ts.seg_base + i] = (uint32_t)i;
-      }
+      keys[ts.seg_base + i] = k;
+      vals[ts.seg_base + i] = (uint32_t)i;
+      // one add per distinct digit of the warp, as in k_radix_hist
+      const uint32_t d = k & 255u;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      if (lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
     }
+    cta_sync();
+    hist[threadIdx.x * tiles + tile] = h[threadIdx.x];
+    cta_sync();
   }
 }
 
-constexpr int kItems = kSortTile / kCtaThreads;   // 16
-constexpr int kWarps = kCtaThreads / 32;          // 8
 
 __global__ void __launch_bounds__(kCtaThreads) k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
                                                            uint32_t* hist, uint32_t tiles) {
@@ -408,7 +422,7 @@ bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
   const uint32_t tiles = (s.n + kSortTile - 1) / kSortTile;
   if (!s.keys_in) {
     int ctas = (int)std::min<uint32_t>(tiles, (uint32_t)grid_ctas);
-    k_sort_init<<<ctas, kCtaThreads, 0, st>>>(t, s.keys_a, s.vals_a, s.tile_scene, s.sentinel, tiles);
+    k_sort_init<<<ctas, kCtaThreads, 0, st>>>(t, s.keys_a, s.vals_a, s.tile_scene, s.sentinel, tiles, s.hist);
   }
   uint32_t *ka = s.keys_a, *va = s.vals_a, *kb = s.keys_b, *vb = s.vals_b;
   for (int p = 0; p < s.passes; p++) {
@@ -416,7 +430,7 @@ bool launch_sort(const TickInfo& t, const SortInfo& s, const uint32_t** perm_out
     int ctas = (int)std::min<uint32_t>(tiles, (uint32_t)grid_ctas);
     const uint32_t* kin = (p == 0 && s.keys_in) ? s.keys_in : ka;
     const uint32_t* vin = (p == 0 && s.keys_in) ? nullptr : va;
-    k_radix_hist<<<ctas, kCtaThreads, 0, st>>>(kin, s.n, shift, s.hist, tiles);
+    if (p > 0 || s.keys_in) k_radix_hist<<<ctas, kCtaThreads, 0, st>>>(kin, s.n, shift, s.hist, tiles);
     if (s.keys_in) {
       k_radix_scan<<<256, kCtaThreads, 0, st>>>(s.hist, tiles, s.digit_total);
       k_radix_scatter<false><<<ctas, kCtaThreads, 0, st>>>(kin, vin, kb, vb, s.n, shift, s.hist, s.digit_total, tiles,
