@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan_seg(uint32_t* hist, 
 // the keys' order in the tile, so equal digits keep their input order. vin == nullptr stands for the
 // identity (the value of key e is e). SEG: the segmented sort, where a tile's digit bases are its
 // scene's segment start plus the exclusive scan of that scene's digit totals.
-// Four CTAs per SM (64 registers; the segmented form spills 20 B): the pass is latency-bound, and
+// Four CTAs per SM (64 registers; the unsegmented form spills 20 B): the pass is latency-bound, and
 // that occupancy made the mixed scene's sort phase 10 % faster than the compiler's 76-91 registers.
 template <bool SEG>
 __global__ void __launch_bounds__(kCtaThreads, 4) k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
