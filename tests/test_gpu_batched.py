@@ -165,3 +165,54 @@ def test_segmented_sort_tile_edges():
         assert all(np.array_equal(x, y) for x, y in zip(a.readBins(), b.readBins())), n
         a.destroy()
     w.destroy()
+
+
+def _water_records():
+    src = make(None, (16, (4, 5, 3), (6, 5, 7), "water", (0.5, -1.0, 0.2)))
+    src.step(dt=src.substepDt, K=2)
+    rec = src.readParticles()
+    src.destroy()
+    return rec
+
+
+def _scene_from(rec, world, n):
+    sim = MPM(world, grid=16, maxParticles=max(n, 1), substeps=8)
+    sim._material("water")
+    if n:
+        assert sim.addRecords(rec[:n]) == n
+    return sim
+
+
+def _check_against_alone(rec, counts, sims, which):
+    for i in which:
+        a = _scene_from(rec, None, counts[i])
+        a.step(dt=a.substepDt, K=8)
+        assert np.array_equal(bits(a.readParticles()), bits(sims[i].readParticles())), i
+        assert all(np.array_equal(x, y) for x, y in zip(a.readBins(), sims[i].readBins())), i
+        a.destroy()
+
+
+def test_more_scenes_than_the_shared_scene_tables():
+    """1,100 scenes in one tick, more than the 1,024 that the kernels' shared-memory scene tables
+    hold: the G2P and the sort find a chunk's scene in the tick table in global memory, and the grid
+    update walks the host's node chunks instead of splitting the regions evenly. Sampled scenes on
+    both sides of the table's size equal the same scenes stepped alone after two sorts."""
+    rec = _water_records()
+    counts = [100 + (i * 37) % (len(rec) - 100) for i in range(1100)]
+    w = World()
+    sims = [_scene_from(rec, w, n) for n in counts]
+    w.step(8)
+    _check_against_alone(rec, counts, sims, [0, 1, 511, 1023, 1024, 1025, 1099])
+    w.destroy()
+
+
+def test_even_grid_split_with_an_empty_scene():
+    """A tick of six scenes, one without particles (an empty region, no nodes in the evenly split
+    grid update) between others of uneven sizes: every scene equals the same scene stepped alone."""
+    rec = _water_records()
+    counts = [700, 0, 1500, 1, 4096 % len(rec), 333]
+    w = World()
+    sims = [_scene_from(rec, w, n) for n in counts]
+    w.step(8)
+    _check_against_alone(rec, counts, sims, range(len(counts)))
+    w.destroy()
