@@ -636,6 +636,7 @@ __device__ __forceinline__ void grid_chunks(const TickInfo& t) {
 // table, which counts whole grids and leaves most chunks empty. Each CTA sums the scenes' region sizes
 // itself (four scenes a thread, then a block scan) into an exclusive prefix in shared memory.
 __device__ __forceinline__ void grid_even(const TickInfo& t) {
+  static_assert(4 * kCtaThreads >= kSceneTable, "four scenes a thread cover the table");
   __shared__ long long pre[kSceneTable + 1];
   __shared__ long long wsum[kCtaThreads / 32];
   const int nsc = t.nscenes;
