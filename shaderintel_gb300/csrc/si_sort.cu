@@ -135,6 +135,10 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
 
 // The segmented form of k_radix_scan: per digit, the exclusive prefix over the tiles of each scene
 // (restarting where tile_scene changes), and each scene's digit total into seg_total[scene][digit].
+// A round covers kScanItems tiles a thread, contiguous: each thread scans its own tiles in registers
+// (all its loads in flight together), one segmented block scan combines the threads' last segments,
+// and a carry takes the running segment into the next round.
+constexpr int kScanItems = 8;
 __global__ void __launch_bounds__(kCtaThreads) k_radix_scan_seg(uint32_t* hist, uint32_t tiles,
                                                                const uint32_t* __restrict__ tile_scene,
                                                                uint32_t* seg_total) {
@@ -146,34 +150,67 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan_seg(uint32_t* hist, 
   if (threadIdx.x == 0) carry = 0;
   cta_sync();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t b = 0; b < tiles; b += kCtaThreads) {
-    const uint32_t i = b + threadIdx.x;
-    const bool in = i < tiles;
-    const uint32_t v = in ? row[i] : 0u;
-    const uint32_t sc = in ? __ldg(&tile_scene[i]) : 0xffffffffu;
-    const bool head = in && (i == 0 || __ldg(&tile_scene[i - 1]) != sc);
-    const bool tail = in && (i + 1 == tiles || __ldg(&tile_scene[i + 1]) != sc);
-    // inclusive segmented scan of (v, head) within the warp
-    uint32_t x = v, f = head ? 1u : 0u;
+  constexpr uint32_t kRound = (uint32_t)kCtaThreads * kScanItems;
+  for (uint32_t b = 0; b < tiles; b += kRound) {
+    const uint32_t i0 = b + (uint32_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], sc[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      const uint32_t i = i0 + k;
+      v[k] = i < tiles ? row[i] : 0u;
+      sc[k] = i < tiles ? __ldg(&tile_scene[i]) : 0xffffffffu;
+    }
+    const uint32_t before = (i0 > 0 && i0 <= tiles) ? __ldg(&tile_scene[i0 - 1]) : 0xffffffffu;
+    const uint32_t after = i0 + kScanItems < tiles ? __ldg(&tile_scene[i0 + kScanItems]) : 0xffffffffu;
+    // the thread's own inclusive scan, restarting at each head (the first tile of a scene)
+    uint32_t x[kScanItems], acc = 0;
+    bool fl = false;   // a head among the thread's tiles so far
+    int first_head = kScanItems;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      const uint32_t i = i0 + k;
+      const bool head = i < tiles && (i == 0 || sc[k] != (k ? sc[k - 1] : before));
+      if (head) {
+        acc = v[k];
+        if (!fl) first_head = k;
+        fl = true;
+      } else {
+        acc += v[k];
+      }
+      x[k] = acc;
+    }
+    // inclusive segmented scan of the threads' (last segment sum, has head) within the warp
+    uint32_t xi = acc, fi = fl ? 1u : 0u;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      const uint32_t g = __shfl_up_sync(0xffffffffu, f, o);
-      if (lane >= o && !f) { x += y; f = g; }
+      const uint32_t y = __shfl_up_sync(0xffffffffu, xi, o);
+      const uint32_t g = __shfl_up_sync(0xffffffffu, fi, o);
+      if (lane >= o && !fi) { xi += y; fi = g; }
     }
-    if (lane == 31) { warp_sum[warp] = x; warp_head[warp] = f; }
+    if (lane == 31) { warp_sum[warp] = xi; warp_head[warp] = fi; }
     cta_sync();
-    // the earlier warps' part of this element's segment, then the carry of the earlier tiles
-    if (!f) {
-      for (int w = warp - 1; w >= 0 && !f; w--) { x += warp_sum[w]; f = warp_head[w]; }
-      if (!f) x += carry;
-    }
-    if (in) {
-      row[i] = x - v;
-      if (tail) seg_total[(size_t)sc * 256 + d] = x;
+    // what flows into the warp: the carry, then the earlier warps in order
+    uint32_t p = carry;
+    for (int w = 0; w < warp; w++) p = warp_head[w] ? warp_sum[w] : p + warp_sum[w];
+    // what flows into this thread: the warp's inflow, then the earlier lanes of the warp
+    const uint32_t e = __shfl_up_sync(0xffffffffu, xi, 1), ef = __shfl_up_sync(0xffffffffu, fi, 1);
+    const uint32_t in = lane == 0 ? p : (ef ? e : p + e);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      const uint32_t i = i0 + k;
+      if (i < tiles) {
+        const uint32_t xk = k < first_head ? in + x[k] : x[k];
+        row[i] = xk - v[k];
+        const bool tail = i + 1 == tiles || sc[k] != (k + 1 < kScanItems ? sc[k + 1] : after);
+        if (tail) seg_total[(size_t)sc[k] * 256 + d] = xk;
+        x[k] = xk;
+      }
     }
     cta_sync();   // every thread has read carry and the warp sums
-    if (i == min(b + kCtaThreads, tiles) - 1) carry = x;   // the block's last tile: its segment goes on
+    const uint32_t last = min(b + kRound, tiles) - 1;  // the round's last tile: its segment goes on
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+      if (i0 + k == last) carry = x[k];
     cta_sync();
   }
 }
