@@ -103,7 +103,9 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_hist(const uint32_t* __re
   }
 }
 
-// one CTA per digit: exclusive scan over the tiles in place, digit total out
+// one CTA per digit: exclusive scan over the tiles in place, digit total out. A round covers
+// kScanItems contiguous tiles a thread, summed in registers, and one block scan of the threads' sums.
+constexpr int kScanItems = 8;
 __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint32_t tiles, uint32_t* digit_total) {
   __shared__ uint32_t warp_sum[kWarps];
   __shared__ uint32_t carry;
@@ -111,10 +113,16 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
   if (threadIdx.x == 0) carry = 0;
   cta_sync();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t b = 0; b < tiles; b += kCtaThreads) {
-    uint32_t i = b + threadIdx.x;
-    uint32_t v = i < tiles ? row[i] : 0u;
-    uint32_t x = v;
+  constexpr uint32_t kRound = (uint32_t)kCtaThreads * kScanItems;
+  for (uint32_t b = 0; b < tiles; b += kRound) {
+    const uint32_t i0 = b + (uint32_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      v[k] = i0 + k < tiles ? row[i0 + k] : 0u;
+      sum += v[k];
+    }
+    uint32_t x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -124,8 +132,13 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
     cta_sync();
     uint32_t wpre = 0, total = 0;
     for (int w = 0; w < kWarps; w++) { uint32_t s = warp_sum[w]; if (w < warp) wpre += s; total += s; }
-    uint32_t c = carry;
-    if (i < tiles) row[i] = c + wpre + x - v;
+    const uint32_t c = carry;
+    uint32_t run = c + wpre + x - sum;   // the tiles before this thread's first
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      if (i0 + k < tiles) row[i0 + k] = run;
+      run += v[k];
+    }
     cta_sync();
     if (threadIdx.x == 0) carry = c + total;
     cta_sync();
@@ -138,7 +151,6 @@ __global__ void __launch_bounds__(kCtaThreads) k_radix_scan(uint32_t* hist, uint
 // A round covers kScanItems tiles a thread, contiguous: each thread scans its own tiles in registers
 // (all its loads in flight together), one segmented block scan combines the threads' last segments,
 // and a carry takes the running segment into the next round.
-constexpr int kScanItems = 8;
 __global__ void __launch_bounds__(kCtaThreads) k_radix_scan_seg(uint32_t* hist, uint32_t tiles,
                                                                const uint32_t* __restrict__ tile_scene,
                                                                uint32_t* seg_total) {
