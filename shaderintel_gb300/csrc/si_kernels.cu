@@ -22,7 +22,10 @@ namespace si {
 // Shared tile: kTileNodes nodes, used first as the gather tile of the G2P (vec4f per node) and then
 // as the P2G scatter tile (four planes of i32, stride kTileNodes, so the four channel atomics of a
 // node share one address computation). TickInfo::tile_nodes (<= kTileNodes) is the usable capacity.
-constexpr int kTileNodes = 2048;
+#ifndef SI_TILE_NODES
+#define SI_TILE_NODES 2048
+#endif
+constexpr int kTileNodes = SI_TILE_NODES;
 
 // CTA barrier that lanes of one warp may reach along different paths (after an `if` on the lane's
 // own particle or a tail loop). __syncthreads() is the warp-aligned barrier (barrier.sync.aligned),

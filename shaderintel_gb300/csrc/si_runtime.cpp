@@ -107,7 +107,7 @@ static int world_init(si_world* w) {
   for (auto& e : w->marks) CK(cudaEventCreate(&e));
   CK(cudaMalloc((void**)&w->grid_done, 4 * sizeof(uint32_t)));   // k_grid's counter, k_g2p's two
   CK(cudaMemset(w->grid_done, 0, 4 * sizeof(uint32_t)));
-  return world_configure(w, w->ppt, w->tile_nodes);
+  return world_configure(w, w->ppt, std::min(w->tile_nodes, max_tile_nodes()));
 }
 
 int world_configure(si_world* w, int ppt, int tile_nodes) {
