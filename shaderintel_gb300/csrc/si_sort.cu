@@ -83,23 +83,35 @@ __global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t*
 __global__ void __launch_bounds__(kCtaThreads) k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
                                                            uint32_t* hist, uint32_t tiles) {
   __shared__ uint32_t h[256];
+  const unsigned lane = threadIdx.x & 31u;
+  // a thread's digits of one tile (256: past the end); the next tile's are loaded while this one's
+  // are counted
+  auto digits = [&](uint32_t tile, uint32_t (&d)[kItems]) {
+#pragma unroll
+    for (int r = 0; r < kItems; r++) {
+      const uint32_t e = tile * kSortTile + r * kCtaThreads + threadIdx.x;
+      d[r] = tile < tiles && e < n ? (__ldg(&keys[e]) >> shift) & 255u : 256u;
+    }
+  };
+  uint32_t d[kItems];
+  digits(blockIdx.x, d);
   for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     h[threadIdx.x] = 0;
     cta_sync();
-    const uint32_t base = tile * kSortTile;
+    uint32_t dn[kItems];
+    digits(tile + gridDim.x, dn);
     // the keys arrive nearly sorted, so most lanes of a warp share a digit: one add per distinct
     // digit of the warp (its lowest lane adds the group's size) instead of one per lane
-    const unsigned lane = threadIdx.x & 31u;
 #pragma unroll
     for (int r = 0; r < kItems; r++) {
-      const uint32_t e = base + r * kCtaThreads + threadIdx.x;
-      const uint32_t d = e < n ? (__ldg(&keys[e]) >> shift) & 255u : 256u;
-      const unsigned peers = __match_any_sync(0xffffffffu, d);
-      if (d < 256u && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d], (uint32_t)__popc(peers));
+      const unsigned peers = __match_any_sync(0xffffffffu, d[r]);
+      if (d[r] < 256u && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[d[r]], (uint32_t)__popc(peers));
     }
     cta_sync();
     hist[threadIdx.x * tiles + tile] = h[threadIdx.x];
     cta_sync();
+#pragma unroll
+    for (int r = 0; r < kItems; r++) d[r] = dn[r];
   }
 }
 
