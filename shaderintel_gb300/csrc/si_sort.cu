@@ -294,13 +294,26 @@ __global__ void __launch_bounds__(kCtaThreads, 4) k_radix_scatter(const uint32_t
     cta_sync();
     const uint32_t wbase = tile * kSortTile + (uint32_t)warp * kSeg;
     uint32_t key[kItems], val[kItems];
+    // SEG: the warp's keys and values are all loaded before the counting (batched substep -0.2 %;
+    // the unsegmented form spills more that way and loads them round by round)
+    if (SEG) {
+#pragma unroll
+      for (int r = 0; r < kItems; r++) {
+        const uint32_t e = wbase + r * 32 + lane;
+        const bool ok = e < n;
+        key[r] = ok ? kin[e] : 0u;
+        val[r] = ok ? (vin ? vin[e] : e) : 0u;
+      }
+    }
     // 1. the warp's digit counts
 #pragma unroll
     for (int r = 0; r < kItems; r++) {
       const uint32_t e = wbase + r * 32 + lane;
       const bool ok = e < n;
-      key[r] = ok ? kin[e] : 0u;
-      val[r] = ok ? (vin ? vin[e] : e) : 0u;
+      if (!SEG) {
+        key[r] = ok ? kin[e] : 0u;
+        val[r] = ok ? (vin ? vin[e] : e) : 0u;
+      }
       const uint32_t d = ok ? (key[r] >> shift) & 255u : 256u;
       const unsigned peers = __match_any_sync(0xffffffffu, d);
       if (ok && (peers & lt_mask) == 0u) woff[warp][d] += (uint32_t)__popc(peers);
