@@ -54,16 +54,23 @@ __global__ void __launch_bounds__(kCtaThreads) k_sort_init(TickInfo t, uint32_t*
     const int first = (int)(slot0 - ts.seg_base);
     const bool from_x = (ts.flags & F_KEYS_FROM_X) != 0;
     const uint32_t nb = from_x ? ts.prm->num_blocks : 0u;
-#pragma unroll 4
+    // stored keys: all sixteen loaded before the counting (positions are read round by round)
+    uint32_t kk[kItems];
+    if (!from_x) {
+#pragma unroll
+      for (int r = 0; r < kItems; r++) {
+        const int i = first + r * kCtaThreads + (int)threadIdx.x;
+        kk[r] = i < n ? __ldg(&ts.keys[i]) : sentinel;
+      }
+    }
+#pragma unroll
     for (int r = 0; r < kItems; r++) {
       const int i = first + r * kCtaThreads + (int)threadIdx.x;
-      uint32_t k = sentinel;
-      if (i < n) {
-        if (from_x) {
+      uint32_t k = from_x ? sentinel : kk[r];
+      if (from_x) {
+        if (i < n) {
           const float4 x = ts.P[i];
           k = block_key(x.x, x.y, x.z, nb);
-        } else {
-          k = __ldg(&ts.keys[i]);
         }
       }
       keys[ts.seg_base + i] = k;
